@@ -1,0 +1,316 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 photon-history transport path.
+
+Workload (one "step"): the heterogeneous cone-beam dose configuration - 256x256x128 voxels
+at 0.5 mm, 40 seeded ellipsoids (soft tissue / adipose / cortical bone) in air, 80 kVp
+Kramers spectrum filtered by 2.5 mm Al, point source 50 cm from the phantom with a 20 degree
+cone, per-voxel dose and variance tally - 1e8 histories through the mixed-precision kernel
+(FP32 transport, 64-bit fixed-point tallies).  Seeded synthetic inputs; nothing is read
+from a dataset.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on rank 0.  --impl reference times the CPU restatement of the reference
+transport (oracle/, all host threads) on bounded samples of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "histories/s per GB300, mixed-precision vs plain at matched dose error; p99 latency"
+UNIT = "histories/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--histories", type=float, default=1e8)
+    p.add_argument("--cpu-sample", type=float, default=1e6, help="histories of the CPU baseline sample")
+    p.add_argument("--quick", action="store_true", help="skip the FP64, e2e and CPU legs")
+    return p.parse_args()
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+        except ImportError:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local, dist
+
+
+def reference_arm(args, world, rank):
+    """CPU restatement of the reference transport, all host threads, bounded samples."""
+    if rank != 0:
+        return
+    import midsx_gb300 as M
+    import oracle
+    from midsx_gb300 import build as B, scenes
+    B.build()
+    sc = scenes.cone_beam_dose(n_histories=int(args.histories))
+    blob = M.TableBlob(sc.materials, e_max=sc.e_max)
+    threads = os.cpu_count() or 1
+    n = int(min(args.cpu_sample, 4e5))
+    times = []
+    for i in range(args.warmup + args.steps):
+        r = oracle.run(blob, n=n, seed=1, first=i * n, rng=oracle.RNG_MT19937, threads=threads, dose=True,
+                       **sc.oracle_kwargs())
+        if i >= args.warmup:
+            times.append(r["run_time"])
+    value = n * len(times) / sum(times)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded ellipsoid phantom, Kramers spectrum)",
+            "config": {"workload": sc.name, "histories_per_step": n, "note": "bounded sample of the 1e8-history step"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d histories per step of %s, mt19937 streams" % (n, sc.name)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        return
+    import numpy as np
+    import torch
+
+    import midsx_gb300 as M
+    from midsx_gb300 import build as B, native as N, scenes
+
+    B.build()
+    torch.cuda.set_device(local)
+    N_hist = int(args.histories)
+    t0 = time.time()
+    sc = scenes.cone_beam_dose(n_histories=N_hist)
+    tables, ph, src, tl = sc.build()
+    log("setup %.1fs (tables %d materials, %d voxels)" % (time.time() - t0, len(sc.materials), ph.n_voxels))
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    base = rank << 40
+
+    def step(i, precision="mixed", n=N_hist, events=None):
+        flush.zero_()
+        if events:
+            events[0].record(stream)
+        tl.reset(sptr)
+        if events:
+            events[1].record(stream)
+        M.run(tables, ph, src, tl, n, seed=1, first=base + i * n, precision=precision, stream=sptr)
+        if events:
+            events[2].record(stream)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for i in range(args.steps):
+        step(args.warmup + i, events=evs[i])
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [e[0].elapsed_time(e[2]) for e in evs]
+    kern_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    total_s = sum(step_ms) / 1e3
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * args.steps * N_hist / total_s
+    st = tl.stats()
+    result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport / int64 fixed-point tallies",
+              "data": "synthetic (seeded ellipsoid phantom, Kramers spectrum)",
+              "config": {"workload": sc.name, "histories_per_step": N_hist, "precision": "mixed",
+                         "voxels": ph.n_voxels, "dose_tally": "count/sum/sumsq per voxel (268 MB)",
+                         "l2": "flushed between steps (256 MB write) and tally > L2",
+                         "parallelism": "replicas over history ranges" if world > 1 else "single GPU"},
+              "clocks": clk, "gpu_launches": args.steps,
+              "step_latency_ms": {"p50": statistics.median(step_ms), "p99": float(np.percentile(step_ms, 99))},
+              "steps_per_history": st["steps"] / st["histories"],
+              "voxel_fetches_per_history": st["voxel_fetches"] / st["histories"]}
+    if rank != 0:
+        return
+    if not args.quick:
+        # plain FP64 form on the same workload and the same Philox streams
+        n64 = max(N_hist // 10, 1000)
+        ev64 = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(2)]
+        step(0, "fp64", n64)
+        for i in range(2):
+            step(1 + i, "fp64", n64, ev64[i])
+        torch.cuda.synchronize()
+        t64 = sum(e[1].elapsed_time(e[2]) for e in ev64) / 1e3
+        plain = 2 * n64 / t64
+        # matched dose error: identical streams through both precisions
+        ncmp = min(N_hist, 2_000_000)
+        doses = {}
+        for p in ("fp64", "mixed"):
+            tl.reset(sptr)
+            M.run(tables, ph, src, tl, ncmp, seed=77, precision=p, stream=sptr)
+            doses[p] = tl.dose(sptr)
+        s64, s32 = doses["fp64"]["sum"].ravel(), doses["mixed"]["sum"].ravel()
+        q64, q32 = doses["fp64"]["sumsq"].ravel(), doses["mixed"]["sumsq"].ravel()
+        sel = s64 > 0.01 * s64.max()
+        z = (s32[sel] - s64[sel]) / np.sqrt(q32[sel] + q64[sel])
+        result["plain_fp64"] = {"value": plain, "unit": UNIT, "histories_per_step": n64,
+                                "mixed_over_plain": value / world / plain}
+        result["matched_dose_error"] = {
+            "histories": ncmp, "total_dose_rel_diff": float(abs(s32.sum() - s64.sum()) / s64.sum()),
+            "voxels_compared": int(sel.sum()), "frac_voxels_beyond_3sigma": float(np.mean(np.abs(z) > 3))}
+        # end to end through the C ABI with host buffers (pinned), copies inside the timing
+        ids_pinned = torch.from_numpy(sc.ids.ravel()).pin_memory()
+        dose_pinned = torch.empty(ph.n_voxels, dtype=torch.float64).pin_memory()
+        e2e_t = []
+        for i in range(1 + args.steps):
+            cfg = M.run_config(N_hist, 1, first=base + (100 + i) * N_hist, precision="mixed")
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            _run_host(M, N, tables, ph.spec, ids_pinned, src.spec, sc, cfg, dose_pinned)
+            t2 = time.perf_counter()
+            if i:
+                e2e_t.append(t2 - t1)
+        result["e2e"] = {"value": N_hist / statistics.mean(e2e_t), "unit": UNIT,
+                         "h2d_bytes_per_step": int(sc.ids.nbytes + 2 * 8 * len(sc.source["spectrum"][0])),
+                         "d2h_bytes_per_step": int(ph.n_voxels * 8 + 128),
+                         "latency_ms": {"p50": 1e3 * statistics.median(e2e_t),
+                                        "p99": 1e3 * float(np.percentile(e2e_t, 99))}}
+        # CPU baseline: the oracle on a bounded sample, all host threads
+        import oracle
+        threads = os.cpu_count() or 1
+        ncpu = int(args.cpu_sample)
+        r = oracle.run(tables.host, n=ncpu, seed=1, rng=oracle.RNG_MT19937, threads=threads, dose=True,
+                       **sc.oracle_kwargs())
+        so = r["stats"]
+        result["cpu_baseline"] = {"value": ncpu / r["run_time"], "unit": UNIT, "cores": threads, "kind": "port",
+                                  "sample": "%d histories of %s (oracle, mt19937 streams)" % (ncpu, sc.name)}
+        F = so["voxel_fetches"] / so["histories"]
+        W = so["tally_words"] / so["histories"]
+    else:
+        F = st["voxel_fetches"] / st["histories"]
+        W = st["tally_words"] / st["histories"]
+    # roofline of the transport kernel: algorithmic bytes = 32 B x (voxel fetches + tally
+    # records) per history, F and W counted by the CPU oracle on this workload
+    b_hist = 32.0 * (F + W)
+    kernel_s = statistics.mean(kern_ms) / 1e3
+    achieved = N_hist * b_hist / kernel_s / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "transport_traffic.json")
+    if os.path.exists(tpath):
+        t = json.load(open(tpath))
+        traffic = float(t["dram_bytes_per_history"]) * N_hist
+    result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                          "bytes_per_history": b_hist, "F": F, "W": W,
+                          "kernel_ms": 1e3 * kernel_s}
+    if "e2e" not in result:
+        result["e2e"] = None
+    print(json.dumps(result), flush=True)
+
+
+def _run_host(M, N, tables, geom, ids_pinned, src_spec, sc, cfg, dose_pinned):
+    import ctypes as C
+    st = N.RunStats()
+    arr = M.tally_specs(sc.specs)
+    N.check(N.load().midsx_gpu_run_host(tables.handle, C.byref(geom), C.c_void_p(ids_pinned.data_ptr()),
+                                        C.byref(src_spec), arr, len(sc.specs), int(sc.dose_mode), C.byref(cfg),
+                                        C.cast(C.c_void_p(dose_pinned.data_ptr()), N.PD), C.byref(st)),
+            "midsx_gpu_run_host")
+    return st
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,309 @@
+/*
+ * midsx_gpu.h - C ABI of the GB300 photon-history transport path.
+ *
+ * This is the boundary between MIDSX's C++ API (ComputationalDomain, InteractionData,
+ * PhotonSource, VolumeTally/SurfaceTally, PhysicsEngine, runSimulation) and the CUDA
+ * kernels that replace the reference's OpenMP history loop.  Plain C types only: no
+ * torch, no C++ classes, no exceptions.  Every function returns a midsx_status; the
+ * C++ layer (include/MIDSX/Core) turns statuses into the reference's exception types.
+ *
+ * Reference interfaces replaced (paths inside the MIDSX repository):
+ *   runSimulation(...)                 include/MIDSX/Core/run_simulation.h:24-27
+ *   PhysicsEngine::transportPhoton     src/MIDSX/Core/physics_engine.cpp:17-79
+ *   InteractionData / MaterialData     src/MIDSX/Core/interaction_data.cpp:3-73,
+ *                                      src/MIDSX/Core/material_data.cpp:9-170
+ *   ComputationalDomain::getVoxel      src/MIDSX/Core/computational_domain.cpp:16-31
+ *   PhotonSource::generatePhoton       src/MIDSX/Core/source.cpp:150-155
+ *   VolumeTally / SurfaceTally         src/MIDSX/Core/volume_tally.cpp, surface_tally.cpp
+ *   Voxel dose (VectorValue per voxel) src/MIDSX/Core/physics_engine.cpp:160-168
+ *
+ * Units follow the reference: lengths in cm, energies in eV, cross sections in 1/cm.
+ * Handles are not thread-safe; distinct handles may be used from distinct threads.
+ * All device work is enqueued on the caller's CUDA stream (`stream`, a cudaStream_t
+ * passed as void*; NULL = legacy default stream).
+ */
+#ifndef MIDSX_GPU_H
+#define MIDSX_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum midsx_status {
+    MIDSX_OK = 0,
+    MIDSX_INVALID_ARG = 1,   /* bad pointer, size, enum or geometry */
+    MIDSX_OOM = 2,           /* host or device allocation failed */
+    MIDSX_TIMEOUT = 3,       /* a host wait passed its deadline */
+    MIDSX_STEP_CAP = 4,      /* some history hit the step or Compton-trial cap (run stats) */
+    MIDSX_TABLE_RANGE = 5,   /* an energy outside the built tables was requested */
+    MIDSX_CUDA_ERROR = 6,    /* a CUDA runtime call failed; see midsx_last_error() */
+    MIDSX_NOT_FOUND = 7,     /* unknown material name or id */
+    MIDSX_IO_ERROR = 8       /* data file missing or malformed */
+} midsx_status;
+
+typedef enum midsx_precision {
+    MIDSX_PREC_FP64 = 0,   /* plain form: FP64 transport, FP64 atomic tallies */
+    MIDSX_PREC_MIXED = 1   /* FP32 transport, 64-bit fixed-point integer tallies */
+} midsx_precision;
+
+#define MIDSX_MAX_MATERIALS 16
+#define MIDSX_MAX_SPECTRUM_BINS 1024
+#define MIDSX_MAX_TALLIES 64
+
+/* ------------------------------------------------------------------ host tables --- */
+/* A LogLogLinear table (src/MIDSX/Core/interpolators.cpp:33-76): node energies x (raw,
+ * searched), log10 x and log10 y.  Fields are offsets into midsx_table_blob.data. */
+typedef struct midsx_lin_table {
+    int64_t x, lx, ly;
+    int32_t n, reserved;
+} midsx_lin_table;
+
+/* A LogLogSpline (src/MIDSX/Core/interpolators.cpp:3-31): cubic B-spline in
+ * u = (log10 E - lx_min) / (lx_max - lx_min) with knots knot_u[n_ctrl + degree + 1] and
+ * control points ctrl[n_ctrl].  knot_e holds 10^(lx_min + u * (lx_max - lx_min)) for each
+ * knot, so that the span is found by comparing raw energies. */
+typedef struct midsx_spline_table {
+    int64_t knot_e, knot_u, ctrl;
+    int32_t n_ctrl, degree;
+    double lx_min, lx_max;
+} midsx_spline_table;
+
+/* PENELOPE RITA tables of the Rayleigh cosine (src/MIDSX/Core/probability_dist.cpp:62-287).
+ * Energy k has rows [idata[row_start + k], idata[row_start + k + 1]) of x, y, a, b. */
+typedef struct midsx_rita_table {
+    int64_t energy, log_energy, row_start, x, y, a, b;
+    int32_t n_energy, n_rows;
+} midsx_rita_table;
+
+typedef struct midsx_material_table {
+    int32_t id;              /* MIDSX material id (uint8 voxel value) */
+    int32_t reserved;
+    double density;          /* g/cm3 */
+    midsx_lin_table total;   /* total macroscopic cross section, 1/cm */
+    midsx_lin_table photo;   /* photoionisation, 1/cm */
+    midsx_lin_table sfunc;   /* incoherent scattering function S(x) */
+    midsx_lin_table ffactor; /* coherent form factor F(x) */
+    midsx_spline_table coh;  /* coherent cross section, 1/cm */
+    midsx_spline_table incoh;/* incoherent cross section, 1/cm */
+    midsx_rita_table rita;   /* Rayleigh cosine sampler */
+} midsx_material_table;
+
+typedef struct midsx_table_blob {
+    int32_t version;
+    int32_t n_materials;
+    double e_max;                 /* RITA tables cover energies up to this (eV) */
+    midsx_lin_table majorant;     /* global majorant mu_max(E), 1/cm */
+    midsx_material_table mat[MIDSX_MAX_MATERIALS];
+    int64_t n_data;
+    double* data;
+    int64_t n_idata;
+    int64_t* idata;
+} midsx_table_blob;
+
+/* Builds the FP64 tables of `n` materials (by MIDSX id, in this order = dense material
+ * index 0..n-1) from the data files in `data_dir` (epdl_photon.bin, materials.txt,
+ * elements.txt).  Replaces InteractionData(material_names) (src/MIDSX/Core/
+ * interaction_data.cpp:3-73).  RITA tables are built for energy nodes up to the first
+ * node >= e_max.  The blob is host memory; free it with midsx_tables_free. */
+midsx_status midsx_tables_build(const char* data_dir, const int32_t* material_ids, int32_t n,
+                                double e_max, midsx_table_blob** out);
+void midsx_tables_free(midsx_table_blob* blob);
+
+/* Material catalogue lookups (replace InteractionDataHelpers::convertMaterial*,
+ * include/MIDSX/Core/material_helpers.h:110-121).  name_out receives up to cap bytes. */
+midsx_status midsx_catalog_id(const char* data_dir, const char* name, int32_t* id_out);
+midsx_status midsx_catalog_name(const char* data_dir, int32_t id, char* name_out, int32_t cap);
+
+/* Host evaluation of the built tables, for checks and for the C++ API getters
+ * (MaterialData::interpolate*, include/MIDSX/Core/material_data.h:95-143).
+ * which: 0 total, 1 photo, 2 coherent (spline), 3 incoherent (spline), 4 S(x), 5 F(x),
+ *        6 majorant (material ignored). */
+midsx_status midsx_tables_eval(const midsx_table_blob* blob, int32_t material, int32_t which,
+                               const double* x, double* y, int64_t n);
+
+const char* midsx_status_string(midsx_status s);
+const char* midsx_last_error(void);
+
+/* ---------------------------------------------------------------- device handles --- */
+typedef struct midsx_gpu_tables* midsx_tables_h;
+typedef struct midsx_gpu_phantom* midsx_phantom_h;
+typedef struct midsx_gpu_source* midsx_source_h;
+typedef struct midsx_gpu_tallies* midsx_tallies_h;
+
+/* Copies the FP64 tables to the device and derives the FP32 copies used by the mixed
+ * path.  Replaces the per-thread table reads of the reference.  Synchronous. */
+midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, midsx_tables_h* out);
+midsx_status midsx_gpu_tables_destroy(midsx_tables_h t);
+
+/* ComputationalDomain with one voxel grid (src/MIDSX/Core/computational_domain.cpp:16-31,
+ * src/MIDSX/Core/voxel_grid.cpp:43-59,119-128): domain box [0, domain], background
+ * material outside the grid, grid of dims[0]*dims[1]*dims[2] uint8 material ids,
+ * x fastest, voxel size `spacing`, lower corner `origin`. */
+typedef struct midsx_geometry_spec {
+    double domain[3];
+    double spacing[3];
+    double origin[3];
+    int32_t dims[3];
+    int32_t background_id;   /* MIDSX material id of the background */
+} midsx_geometry_spec;
+
+/* Uploads voxel material ids (MIDSX ids, `ids` is host memory) and remaps them to the
+ * dense material index of `tables` on the device.  Fails with MIDSX_NOT_FOUND if a voxel
+ * id is not among the tables' materials.  Synchronous. */
+midsx_status midsx_gpu_phantom_create(midsx_tables_h tables, const midsx_geometry_spec* geom,
+                                      const uint8_t* ids, midsx_phantom_h* out);
+midsx_status midsx_gpu_phantom_destroy(midsx_phantom_h p);
+
+/* PhotonSource (src/MIDSX/Core/source.cpp:44-155).  Geometry is a point (PointGeometry).
+ * Directionality:
+ *   BEAM:        a = pass-through point
+ *   ISOTROPIC:   theta ~ U[0,pi], phi ~ U[0,2pi)  (the reference's definition)
+ *   RECTANGLE:   a = corner, b = edge1, c = edge2 (edges orthogonal)
+ *   DISC:        a = center, b = normal, radius; r ~ U[0,R], theta ~ U[0,2pi)
+ * Spectrum: MONO (mono_energy) or POLY (n_bins energies with probabilities,
+ * DiscreteInversion of src/MIDSX/Core/probability_dist.cpp:11-60). */
+typedef enum midsx_direction_kind {
+    MIDSX_DIR_BEAM = 0, MIDSX_DIR_ISOTROPIC = 1, MIDSX_DIR_RECTANGLE = 2, MIDSX_DIR_DISC = 3
+} midsx_direction_kind;
+typedef enum midsx_spectrum_kind { MIDSX_SPEC_MONO = 0, MIDSX_SPEC_POLY = 1 } midsx_spectrum_kind;
+
+typedef struct midsx_source_spec {
+    double position[3];
+    int32_t direction_kind;
+    int32_t spectrum_kind;
+    double a[3], b[3], c[3];
+    double radius;
+    double mono_energy;
+    int32_t n_bins;
+    int32_t reserved;
+    const double* bin_energy;    /* host pointers, n_bins each */
+    const double* bin_prob;
+} midsx_source_spec;
+
+midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, midsx_source_h* out);
+midsx_status midsx_gpu_source_destroy(midsx_source_h s);
+
+/* Tallies.  Scalar tallies hold, per scatter class (primary, single coherent, single
+ * incoherent, multiple - src/MIDSX/Core/volume_quantity.cpp:53-67), count / sum / sum of
+ * squares of each vector quantity and a count for each count quantity:
+ *   surface (DISC: a = center, b = unit normal, radius; RECT: a = corner, b = edge1,
+ *   c = edge2): IncidentEnergy[3x4], EntranceCosine[3x4], NumberOfPhotons[4]
+ *   volume (AACUBOID: a = min corner, b = max corner):
+ *   EnergyDeposition[3x4], IncidentEnergy[3x4], NumberOfPhotons[4], NumberOfInteractions[4]
+ * BINNED_RECT is a RECT split into nu x nv bins (bin (i,j) equals a RectangularSurfaceTally
+ * over that cell); per bin and class it holds the incident energy sum and photon count.
+ * The voxel dose tally (per grid voxel: deposit count, sum, sum of squares - the summary
+ * of the reference's Voxel::dose VectorValue) is enabled by dose_mode. */
+typedef enum midsx_tally_kind {
+    MIDSX_TALLY_SURFACE_DISC = 1,
+    MIDSX_TALLY_SURFACE_RECT = 2,
+    MIDSX_TALLY_SURFACE_BINNED_RECT = 3,
+    MIDSX_TALLY_VOLUME_AACUBOID = 4
+} midsx_tally_kind;
+
+typedef enum midsx_dose_mode {
+    MIDSX_DOSE_OFF = 0,
+    MIDSX_DOSE_SUM = 1,      /* energy sum per voxel only */
+    MIDSX_DOSE_FULL = 2      /* count, sum and sum of squares per voxel */
+} midsx_dose_mode;
+
+typedef struct midsx_tally_spec {
+    int32_t kind;
+    int32_t nu, nv;          /* bins of a BINNED_RECT along edge1, edge2 */
+    int32_t reserved;
+    double a[3], b[3], c[3];
+    double radius;
+} midsx_tally_spec;
+
+#define MIDSX_SCALAR_SLOTS 40  /* doubles returned per scalar tally, see midsx_gpu_fetch_scalar */
+
+midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const midsx_tally_spec* specs,
+                                      int32_t n_specs, int32_t dose_mode, midsx_tallies_h* out);
+midsx_status midsx_gpu_tallies_destroy(midsx_tallies_h t);
+/* Zeroes every accumulator and the run statistics (enqueued on stream). */
+midsx_status midsx_gpu_tallies_reset(midsx_tallies_h t, void* stream);
+
+typedef struct midsx_run_config {
+    int32_t precision;           /* midsx_precision */
+    int32_t max_steps;           /* per-history step cap (0 = 1000000) */
+    int32_t max_compton_trials;  /* Kahn/S(x) rejection cap (0 = 100000) */
+    int32_t block_size;          /* 0 = tuned default */
+    int32_t blocks_per_sm;       /* 0 = tuned default */
+    int32_t reserved;
+    uint64_t seed;
+    uint64_t first_history;      /* history ids [first, first + n) select Philox streams */
+    uint64_t n_histories;
+} midsx_run_config;
+
+/* Transports n_histories photons and accumulates into `tallies` (asynchronous on stream).
+ * Replaces runSimulation's history loop (src/MIDSX/Core/run_simulation.cpp:13-35).
+ * Random numbers: Philox4x32-10 keyed by seed, one counter stream per history id, so a
+ * run split into several calls over disjoint history ranges equals one call. */
+midsx_status midsx_gpu_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_source_h source,
+                           midsx_tallies_h tallies, const midsx_run_config* cfg, void* stream);
+
+typedef struct midsx_run_stats {
+    uint64_t histories;
+    uint64_t steps;              /* Woodcock steps, including the final escaping one */
+    uint64_t voxel_fetches;      /* steps that landed inside the voxel grid */
+    uint64_t photo, coherent, incoherent;
+    uint64_t compton_trials;
+    uint64_t step_cap_hits, compton_cap_hits, edge_clamps;
+    uint64_t tally_words;        /* tally accumulator updates (atomics issued) */
+    double source_energy;        /* eV, sum over histories */
+    double deposited_grid;       /* eV deposited in grid voxels */
+    double deposited_background; /* eV deposited outside the grid */
+    double escaped_energy;       /* eV carried out of the domain */
+} midsx_run_stats;
+
+/* The fetch functions synchronise `stream` and copy to host memory. */
+midsx_status midsx_gpu_fetch_stats(midsx_tallies_h t, midsx_run_stats* out, void* stream);
+/* Voxel dose: any of the three outputs may be NULL; each has n_voxels entries. */
+midsx_status midsx_gpu_fetch_dose(midsx_tallies_h t, double* sum, double* sumsq, double* count,
+                                  void* stream);
+/* Scalar tally `index` (0-based among the specs): MIDSX_SCALAR_SLOTS doubles, layout
+ * [q][class][n, sum, sumsq] for the two vector quantities (24 values) followed by
+ * [q][class] counts for the count quantities (8 values; surfaces use the first 4). */
+midsx_status midsx_gpu_fetch_scalar(midsx_tallies_h t, int32_t index, double* out, void* stream);
+/* Binned surface tally `index`: energy[nu*nv*4] (eV, [bin_v][bin_u][class]) and
+ * count[nu*nv*4]. */
+midsx_status midsx_gpu_fetch_binned(midsx_tallies_h t, int32_t index, double* energy,
+                                    double* count, void* stream);
+
+/* One call from host memory to host memory: uploads the phantom ids, runs, and reads the
+ * dose sum and statistics back (the end-to-end form used by the C++ runSimulation). */
+midsx_status midsx_gpu_run_host(midsx_tables_h tables, const midsx_geometry_spec* geom,
+                                const uint8_t* ids, const midsx_source_spec* source,
+                                const midsx_tally_spec* specs, int32_t n_specs, int32_t dose_mode,
+                                const midsx_run_config* cfg, double* dose_sum_out,
+                                midsx_run_stats* stats_out);
+
+/* ----------------------------------------------------------- sampler diagnostics --- */
+/* Draw n samples of one sampler on the device with the transport kernel's own device
+ * functions and Philox streams (history id = first + i, draw counter from 0).  Used by the
+ * KS tests against the CPU samplers (reference check: tests/distributions/distributions.cpp).
+ * kind: 0 Rayleigh cos(theta) (RITA), 1 Compton (out0 = cos theta, out1 = E'/E),
+ *       2 free path in `material` at energy E (out0 = s, cm), 3 table index of the
+ *       majorant / material total / S(x) / RITA lookups for the given energies (out0..). */
+midsx_status midsx_gpu_sample(midsx_tables_h tables, int32_t precision, int32_t kind,
+                              int32_t material, double energy, uint64_t seed, uint64_t first,
+                              int64_t n, double* out0, double* out1);
+/* Runs cfg->n_histories histories without tallies and writes, per history, the energy
+ * deposited in grid voxels (hist_dep, host memory).  Used to compare trajectories history
+ * by history with the CPU oracle driven by the same Philox streams.  Synchronous. */
+midsx_status midsx_gpu_trace_deposits(midsx_tables_h tables, midsx_phantom_h phantom,
+                                      midsx_source_h source, const midsx_run_config* cfg,
+                                      double* hist_dep);
+/* Table indices found on the device for energies e[n] (FP64 path): idx[6*n] = majorant,
+ * material total, S(x) at x = e (as momentum transfer), coherent-spline span,
+ * incoherent-spline span, RITA energy row. */
+midsx_status midsx_gpu_table_index(midsx_tables_h tables, int32_t material, const double* e,
+                                   int64_t n, int64_t* idx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MIDSX_GPU_H */

@@ -1,0 +1,352 @@
+"""Python view of the C ABI: table building, device handles, runs and result fetches.
+
+Mirrors the reference's objects for the transport path:
+  InteractionData(material names)  -> Tables(material ids or names)
+  ComputationalDomain + VoxelGrid  -> Phantom(domain, spacing, origin, ids, background)
+  PhotonSource(spectrum, direction, PointGeometry) -> Source
+  VolumeTally / SurfaceTally       -> Tallies(spec list), plus the voxel dose tally
+  runSimulation(...)               -> run(...)
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import native as N
+
+DATA_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+WHICH = {"total": 0, "photo": 1, "coherent": 2, "incoherent": 3, "sfunc": 4, "ffactor": 5, "majorant": 6}
+
+
+def material_id(name, data_dir=DATA_DIR):
+    lib = N.load()
+    out = C.c_int32()
+    N.check(lib.midsx_catalog_id(data_dir.encode(), name.encode(), C.byref(out)), "midsx_catalog_id")
+    return out.value
+
+
+def material_name(mid, data_dir=DATA_DIR):
+    lib = N.load()
+    buf = C.create_string_buffer(256)
+    N.check(lib.midsx_catalog_name(data_dir.encode(), int(mid), buf, 256), "midsx_catalog_name")
+    return buf.value.decode()
+
+
+class TableBlob:
+    """Host FP64 tables of a material list (InteractionData)."""
+
+    def __init__(self, materials, e_max=150e3, data_dir=DATA_DIR):
+        lib = N.load()
+        ids = [m if isinstance(m, int) else material_id(m, data_dir) for m in materials]
+        arr = (C.c_int32 * len(ids))(*ids)
+        ptr = C.POINTER(N.TableBlob)()
+        N.check(lib.midsx_tables_build(data_dir.encode(), arr, len(ids), float(e_max), C.byref(ptr)),
+                "midsx_tables_build")
+        self.ptr = ptr
+        self.ids = ids
+        self.e_max = float(e_max)
+
+    @property
+    def blob(self):
+        return self.ptr.contents
+
+    def array(self, off, n):
+        return np.ctypeslib.as_array(self.blob.data, shape=(self.blob.n_data,))[off:off + n]
+
+    def iarray(self, off, n):
+        return np.ctypeslib.as_array(self.blob.idata, shape=(self.blob.n_idata,))[off:off + n]
+
+    def eval(self, material, which, x):
+        lib = N.load()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        w = WHICH[which] if isinstance(which, str) else int(which)
+        N.check(lib.midsx_tables_eval(self.ptr, int(material), w, N.dptr(x), N.dptr(y), x.size),
+                "midsx_tables_eval")
+        return y
+
+    def dense_index(self, mid):
+        return self.ids.index(mid)
+
+    def close(self):
+        if self.ptr:
+            N.load().midsx_tables_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Tables:
+    """FP64 host tables plus their device copy (FP64 + FP32)."""
+
+    def __init__(self, materials, e_max=150e3, data_dir=DATA_DIR, blob=None):
+        self.host = blob if blob is not None else TableBlob(materials, e_max, data_dir)
+        lib = N.load()
+        h = C.c_void_p()
+        N.check(lib.midsx_gpu_tables_create(self.host.ptr, C.byref(h)), "midsx_gpu_tables_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            N.load().midsx_gpu_tables_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def geometry_spec(domain, spacing, origin, dims, background_id):
+    g = N.GeometrySpec()
+    g.domain = N.vec3(domain)
+    g.spacing = N.vec3(spacing)
+    g.origin = N.vec3(origin)
+    g.dims = N.I3(*[int(d) for d in dims])
+    g.background_id = int(background_id)
+    return g
+
+
+class Phantom:
+    """One voxel grid inside a box domain.  ids: uint8 MIDSX material ids shaped (nz, ny, nx)
+    (x fastest, the reference's voxel numbering)."""
+
+    def __init__(self, tables, domain, spacing, origin, ids, background_id):
+        ids = np.ascontiguousarray(ids, dtype=np.uint8)
+        if ids.ndim != 3:
+            raise ValueError("ids must be a 3-D array shaped (nz, ny, nx)")
+        nz, ny, nx = ids.shape
+        self.dims = (nx, ny, nz)
+        self.spec = geometry_spec(domain, spacing, origin, self.dims, background_id)
+        self.ids = ids
+        lib = N.load()
+        h = C.c_void_p()
+        N.check(lib.midsx_gpu_phantom_create(tables.handle, C.byref(self.spec), ids.ctypes.data, C.byref(h)),
+                "midsx_gpu_phantom_create")
+        self.handle = h
+
+    @property
+    def n_voxels(self):
+        return int(np.prod(self.dims))
+
+    def close(self):
+        if self.handle:
+            N.load().midsx_gpu_phantom_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def source_spec(position, direction, energy=None, spectrum=None):
+    """direction: ("beam", through) | ("isotropic",) | ("rect", corner, e1, e2) |
+    ("disc", center, normal, radius).  energy: mono energy in eV, or spectrum=(energies, probs)."""
+    s = N.SourceSpec()
+    s.position = N.vec3(position)
+    kind = direction[0]
+    if kind == "beam":
+        s.direction_kind = N.DIR_BEAM
+        s.a = N.vec3(direction[1])
+    elif kind == "isotropic":
+        s.direction_kind = N.DIR_ISOTROPIC
+    elif kind == "rect":
+        s.direction_kind = N.DIR_RECTANGLE
+        s.a, s.b, s.c = N.vec3(direction[1]), N.vec3(direction[2]), N.vec3(direction[3])
+    elif kind == "disc":
+        s.direction_kind = N.DIR_DISC
+        s.a, s.b = N.vec3(direction[1]), N.vec3(direction[2])
+        s.radius = float(direction[3])
+    else:
+        raise ValueError("unknown direction kind %r" % (kind,))
+    keep = []
+    if spectrum is not None:
+        e = np.ascontiguousarray(spectrum[0], dtype=np.float64)
+        p = np.ascontiguousarray(spectrum[1], dtype=np.float64)
+        s.spectrum_kind = N.SPEC_POLY
+        s.n_bins = e.size
+        s.bin_energy = N.dptr(e)
+        s.bin_prob = N.dptr(p)
+        keep = [e, p]
+    else:
+        s.spectrum_kind = N.SPEC_MONO
+        s.mono_energy = float(energy)
+    s._keep = keep
+    return s
+
+
+class Source:
+    def __init__(self, position, direction, energy=None, spectrum=None):
+        self.spec = source_spec(position, direction, energy, spectrum)
+        self.max_energy = float(np.max(spectrum[0])) if spectrum is not None else float(energy)
+        lib = N.load()
+        h = C.c_void_p()
+        N.check(lib.midsx_gpu_source_create(C.byref(self.spec), C.byref(h)), "midsx_gpu_source_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            N.load().midsx_gpu_source_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tally_specs(specs):
+    """specs: list of dicts {kind: 'disc'|'rect'|'binned'|'cuboid', ...}."""
+    arr = (N.TallySpec * max(1, len(specs)))()
+    for i, d in enumerate(specs):
+        t = arr[i]
+        k = d["kind"]
+        if k == "disc":
+            t.kind = N.TALLY_DISC
+            t.a, t.b, t.radius = N.vec3(d["center"]), N.vec3(d["normal"]), float(d["radius"])
+        elif k in ("rect", "binned"):
+            t.kind = N.TALLY_RECT if k == "rect" else N.TALLY_BINNED_RECT
+            t.a, t.b, t.c = N.vec3(d["corner"]), N.vec3(d["edge1"]), N.vec3(d["edge2"])
+            if k == "binned":
+                t.nu, t.nv = int(d["nu"]), int(d["nv"])
+        elif k == "cuboid":
+            t.kind = N.TALLY_AACUBOID
+            t.a, t.b = N.vec3(d["min"]), N.vec3(d["max"])
+        else:
+            raise ValueError("unknown tally kind %r" % (k,))
+    return arr
+
+
+class Tallies:
+    def __init__(self, phantom, specs=(), dose_mode=N.DOSE_FULL):
+        self.specs = list(specs)
+        self.dose_mode = dose_mode
+        self.phantom = phantom
+        arr = tally_specs(self.specs)
+        lib = N.load()
+        h = C.c_void_p()
+        N.check(lib.midsx_gpu_tallies_create(phantom.handle if phantom is not None else None, arr,
+                                             len(self.specs), int(dose_mode), C.byref(h)),
+                "midsx_gpu_tallies_create")
+        self.handle = h
+
+    def reset(self, stream=None):
+        N.check(N.load().midsx_gpu_tallies_reset(self.handle, stream), "midsx_gpu_tallies_reset")
+
+    def stats(self, stream=None, allow_cap=True):
+        st = N.RunStats()
+        N.check(N.load().midsx_gpu_fetch_stats(self.handle, C.byref(st), stream), "midsx_gpu_fetch_stats",
+                allow=(N.STEP_CAP,) if allow_cap else ())
+        return st.as_dict()
+
+    def dose(self, stream=None):
+        n = self.phantom.n_voxels
+        s = np.empty(n)
+        full = self.dose_mode == N.DOSE_FULL
+        s2 = np.empty(n) if full else None
+        c = np.empty(n) if full else None
+        N.check(N.load().midsx_gpu_fetch_dose(self.handle, N.dptr(s), N.dptr(s2) if full else None,
+                                              N.dptr(c) if full else None, stream), "midsx_gpu_fetch_dose")
+        shape = self.phantom.ids.shape
+        out = {"sum": s.reshape(shape)}
+        if full:
+            out["sumsq"] = s2.reshape(shape)
+            out["count"] = c.reshape(shape)
+        return out
+
+    def scalar(self, i, stream=None):
+        out = np.empty(N.SCALAR_SLOTS)
+        N.check(N.load().midsx_gpu_fetch_scalar(self.handle, int(i), N.dptr(out), stream), "midsx_gpu_fetch_scalar")
+        return out
+
+    def binned(self, i, stream=None):
+        d = self.specs[i]
+        n = d["nu"] * d["nv"] * 4
+        e = np.empty(n)
+        c = np.empty(n)
+        N.check(N.load().midsx_gpu_fetch_binned(self.handle, int(i), N.dptr(e), N.dptr(c), stream),
+                "midsx_gpu_fetch_binned")
+        return e.reshape(d["nv"], d["nu"], 4), c.reshape(d["nv"], d["nu"], 4)
+
+    def close(self):
+        if self.handle:
+            N.load().midsx_gpu_tallies_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+PRECISIONS = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}
+
+
+def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0):
+    c = N.RunConfig()
+    c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    c.n_histories = int(n)
+    c.seed = int(seed)
+    c.first_history = int(first)
+    c.block_size = int(block)
+    c.blocks_per_sm = int(per_sm)
+    c.max_steps = int(max_steps)
+    c.max_compton_trials = int(max_trials)
+    return c
+
+
+def run(tables, phantom, source, tallies, n, seed, first=0, precision="mixed", stream=None, **kw):
+    """Enqueue n histories (asynchronous on `stream`, a cudaStream_t as int or None)."""
+    cfg = run_config(n, seed, first, precision, **kw)
+    N.check(N.load().midsx_gpu_run(tables.handle, phantom.handle, source.handle, tallies.handle, C.byref(cfg),
+                                   stream), "midsx_gpu_run")
+
+
+def trace_deposits(tables, phantom, source, n, seed, first=0, precision="fp64", **kw):
+    cfg = run_config(n, seed, first, precision, **kw)
+    out = np.empty(int(n))
+    N.check(N.load().midsx_gpu_trace_deposits(tables.handle, phantom.handle, source.handle, C.byref(cfg),
+                                              N.dptr(out)), "midsx_gpu_trace_deposits")
+    return out
+
+
+def sample(tables, kind, material, energy, n, seed, first=0, precision="fp64"):
+    """Device sampler diagnostics: kind 'rayleigh' | 'compton' | 'freepath'."""
+    k = {"rayleigh": 0, "compton": 1, "freepath": 2}[kind]
+    o0 = np.empty(int(n))
+    o1 = np.empty(int(n))
+    p = PRECISIONS[precision]
+    N.check(N.load().midsx_gpu_sample(tables.handle, p, k, int(material), float(energy), int(seed), int(first),
+                                      int(n), N.dptr(o0), N.dptr(o1)), "midsx_gpu_sample")
+    return (o0, o1) if k == 1 else o0
+
+
+def table_index(tables, material, energies):
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    idx = np.empty(6 * e.size, dtype=np.int64)
+    N.check(N.load().midsx_gpu_table_index(tables.handle, int(material), N.dptr(e), e.size,
+                                           idx.ctypes.data_as(N.PI64)), "midsx_gpu_table_index")
+    return idx.reshape(e.size, 6)
+
+
+def run_host(tables, geom_spec, ids, source_spec_, specs, dose_mode, cfg):
+    """End-to-end call from host buffers (midsx_gpu_run_host); returns (dose_sum, stats)."""
+    ids = np.ascontiguousarray(ids, dtype=np.uint8)
+    dose = np.empty(ids.size) if dose_mode else None
+    st = N.RunStats()
+    arr = tally_specs(specs)
+    N.check(N.load().midsx_gpu_run_host(tables.handle, C.byref(geom_spec), ids.ctypes.data, C.byref(source_spec_),
+                                        arr, len(specs), int(dose_mode), C.byref(cfg),
+                                        N.dptr(dose) if dose is not None else None, C.byref(st)),
+            "midsx_gpu_run_host")
+    return dose, st.as_dict()

@@ -1,0 +1,293 @@
+// device.cuh - device functions of the photon-history transport kernels.
+//
+// Every function states the reference code it restates (paths inside MIDSX):
+//   free path, delta test            src/MIDSX/Core/physics_engine.cpp:170-183
+//   interaction type                 src/MIDSX/Core/physics_engine.cpp:82-109
+//   photoelectric / Rayleigh / Compton
+//                                    src/MIDSX/Core/photon_interactions.cpp:43-141
+//   direction rotation               src/MIDSX/Core/particle.cpp:7-45
+//   source sampling                  src/MIDSX/Core/source.cpp:44-155,
+//                                    src/MIDSX/Core/probability_dist.cpp:18-28
+//   surface / volume tallies         src/MIDSX/Core/surface_tally.cpp:5-112,
+//                                    src/MIDSX/Core/volume_tally.cpp:5-91
+//   quantity classification          src/MIDSX/Core/volume_quantity.cpp:53-67,
+//                                    src/MIDSX/Core/surface_quantity.cpp:49-63
+#pragma once
+#include <stdint.h>
+
+#include "../../include/midsx_gpu.h"
+#include "lookup.h"
+
+namespace midsx {
+
+// -------------------------------------------------------------------- constants ---
+// include/MIDSX/Core/constants.h:13-23
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kMec2 = 0.51099895000E6;  // eV
+constexpr double kEps = 1e-9;
+// ALPHA = mec2 / (sqrt(2) h c 1e8), 1/Angstrom; evaluated on the host in FP64 and
+// passed to the kernels.
+
+// ----------------------------------------------------------------- Philox4x32-10 ---
+// Counter-based generator of Salmon, Moraes, Dror and Shaw, "Parallel random numbers:
+// as easy as 1, 2, 3" (SC'11): 10 rounds of the Philox S-box with multipliers
+// 0xD2511F53 / 0xCD9E8D57 and Weyl key increments 0x9E3779B9 / 0xBB67AE85.
+struct Philox4 {
+    uint32_t v[4];
+};
+
+MIDSX_HD void mulhilo32(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
+#if defined(__CUDA_ARCH__)
+    lo = a * b;
+    hi = __umulhi(a, b);
+#else
+    uint64_t p = uint64_t(a) * uint64_t(b);
+    lo = uint32_t(p);
+    hi = uint32_t(p >> 32);
+#endif
+}
+
+MIDSX_HD Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                               uint32_t k1) {
+    uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint32_t hi0, lo0, hi1, lo1;
+        mulhilo32(0xD2511F53u, x0, hi0, lo0);
+        mulhilo32(0xCD9E8D57u, x2, hi1, lo1);
+        uint32_t y0 = hi1 ^ x1 ^ k0;
+        uint32_t y2 = hi0 ^ x3 ^ k1;
+        x0 = y0;
+        x1 = lo1;
+        x2 = y2;
+        x3 = lo0;
+    }
+    Philox4 o;
+    o.v[0] = x0;
+    o.v[1] = x1;
+    o.v[2] = x2;
+    o.v[3] = x3;
+    return o;
+}
+
+// One random stream per history: draw n uses 64 bits of Philox block (n >> 1) with
+// counter (n >> 1, history_lo, history_hi, 0) and key (seed_lo, seed_hi).  The FP64 path
+// uses the top 53 bits, the FP32 path the top 24 bits of the same 64-bit word, so both
+// precisions consume identical streams.
+struct HistoryRng {
+    uint32_t k0, k1, h0, h1;
+    uint32_t n;
+    uint32_t b0, b1;
+
+    MIDSX_HD void init(uint64_t seed, uint64_t history) {
+        k0 = uint32_t(seed);
+        k1 = uint32_t(seed >> 32);
+        h0 = uint32_t(history);
+        h1 = uint32_t(history >> 32);
+        n = 0;
+        b0 = b1 = 0;
+    }
+    MIDSX_HD uint64_t next64() {
+        uint64_t r;
+        if (n & 1u) {
+            r = (uint64_t(b0) << 32) | b1;
+        } else {
+            Philox4 w = philox4x32_10(n >> 1, h0, h1, 0u, k0, k1);
+            b0 = w.v[2];
+            b1 = w.v[3];
+            r = (uint64_t(w.v[0]) << 32) | w.v[1];
+        }
+        ++n;
+        return r;
+    }
+};
+
+// Uniform in (0, 1].
+MIDSX_HD double to_uniform(uint64_t r, double) { return double((r >> 11) + 1) * 0x1.0p-53; }
+MIDSX_HD float to_uniform(uint64_t r, float) { return float(uint32_t(r >> 40) + 1u) * 0x1.0p-24f; }
+
+template <typename R>
+MIDSX_HD R uniform(HistoryRng& rng) {
+    return to_uniform(rng.next64(), R(0));
+}
+
+// ------------------------------------------------------------------------ vectors ---
+template <typename R>
+struct V3 {
+    R x, y, z;
+};
+
+template <typename R>
+MIDSX_HD R dot(const V3<R>& a, const V3<R>& b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+MIDSX_HD double acos_(double v) { return acos(v); }
+MIDSX_HD float acos_(float v) { return acosf(v); }
+MIDSX_HD void sincos_(double v, double* s, double* c) {
+#if defined(__CUDA_ARCH__)
+    sincos(v, s, c);
+#else
+    *s = sin(v);
+    *c = cos(v);
+#endif
+}
+MIDSX_HD void sincos_(float v, float* s, float* c) {
+#if defined(__CUDA_ARCH__)
+    sincosf(v, s, c);
+#else
+    *s = sinf(v);
+    *c = cosf(v);
+#endif
+}
+MIDSX_HD double fabs_(double v) { return fabs(v); }
+MIDSX_HD float fabs_(float v) { return fabsf(v); }
+
+// ParticleHelpers::rotateDirection: rotate v by theta about the unit vector perpendicular
+// to v built from its smallest component, then by phi about v, as the quaternion product
+// q = q_phi * q_theta applied as q v q^-1 (particle.cpp:7-45).
+template <typename R>
+MIDSX_HD V3<R> rotate_direction(const V3<R>& v, R theta, R phi) {
+    V3<R> p;
+    R ax = fabs_(v.x), ay = fabs_(v.y), az = fabs_(v.z);
+    if (ax <= ay && ax <= az) {
+        p = {R(0), -v.z, v.y};
+    } else if (ay <= az) {
+        p = {v.z, R(0), -v.x};
+    } else {
+        p = {-v.y, v.x, R(0)};
+    }
+    R pn = sqrt_(dot(p, p));
+    if (pn > R(0)) {
+        p.x /= pn;
+        p.y /= pn;
+        p.z /= pn;
+    }
+    R st, ct, sp, cp;
+    sincos_(theta / R(2), &st, &ct);
+    sincos_(phi / R(2), &sp, &cp);
+    // q_theta = (ct, p st), q_phi = (cp, v sp)
+    R tw = ct, tx = p.x * st, ty = p.y * st, tz = p.z * st;
+    R fw = cp, fx = v.x * sp, fy = v.y * sp, fz = v.z * sp;
+    // q = q_phi * q_theta
+    R qw = fw * tw - fx * tx - fy * ty - fz * tz;
+    R qx = fw * tx + fx * tw + fy * tz - fz * ty;
+    R qy = fw * ty - fx * tz + fy * tw + fz * tx;
+    R qz = fw * tz + fx * ty - fy * tx + fz * tw;
+    // r = q * (0, v)
+    R rw = -qx * v.x - qy * v.y - qz * v.z;
+    R rx = qw * v.x + qy * v.z - qz * v.y;
+    R ry = qw * v.y - qx * v.z + qz * v.x;
+    R rz = qw * v.z + qx * v.y - qy * v.x;
+    // q^-1 = conj(q) / |q|^2
+    R n2 = qw * qw + qx * qx + qy * qy + qz * qz;
+    R iw = qw / n2, ix = -qx / n2, iy = -qy / n2, iz = -qz / n2;
+    // out = r * q^-1 (vector part)
+    V3<R> o;
+    o.x = rw * ix + rx * iw + ry * iz - rz * iy;
+    o.y = rw * iy - rx * iz + ry * iw + rz * ix;
+    o.z = rw * iz + rx * iy - ry * ix + rz * iw;
+    return o;
+}
+
+// ----------------------------------------------------------------- device tables ---
+struct DevLin {
+    int x, lx, ly, n;
+};
+struct DevSpline {
+    int knot_e, knot_u, ctrl, n_ctrl, degree;
+    double lx_min, lx_max;
+};
+struct DevRita {
+    int energy, log_energy, row_start, x, y, a, b, n_energy;
+};
+struct DevMaterial {
+    DevLin total, sfunc;
+    DevSpline coh, incoh;
+    DevRita rita;
+};
+struct DevTables {
+    const double* d;     // FP64 data (blob layout)
+    const float* f;      // FP32 copy, same offsets
+    const int* rows;     // RITA row starts
+    int n_materials;
+    double alpha;        // 1/Angstrom per unit k
+    double e_max;
+    DevLin majorant;
+    DevMaterial mat[MIDSX_MAX_MATERIALS];
+};
+
+template <typename R>
+MIDSX_HD const R* tab(const DevTables& t);
+template <>
+MIDSX_HD const double* tab<double>(const DevTables& t) {
+    return t.d;
+}
+template <>
+MIDSX_HD const float* tab<float>(const DevTables& t) {
+    return t.f;
+}
+
+template <typename R>
+MIDSX_HD R lin_lookup(const DevTables& t, const DevLin& L, R q) {
+    const R* D = tab<R>(t);
+    return lin_eval(D + L.x, D + L.lx, D + L.ly, L.n, q);
+}
+
+template <typename R>
+MIDSX_HD R spline_lookup(const DevTables& t, const DevSpline& S, R e) {
+    const R* D = tab<R>(t);
+    int span = spline_span(D + S.knot_e, S.n_ctrl, S.degree, e);
+    return spline_eval_at(D + S.knot_u, D + S.ctrl, S.degree, span, R(S.lx_min), R(S.lx_max), e);
+}
+
+// ContinuousInversion::sample (probability_dist.cpp:73-88).  Returns false if E has no
+// bracketing energy pair (outside the built tables).
+template <typename R>
+MIDSX_HD bool rita_sample(const DevTables& t, const DevRita& T, R E, R y, R& mu) {
+    const R* D = tab<R>(t);
+    int lower = lower_index(D + T.energy, 0, T.n_energy, E) - 1;
+    int upper = lower + 1;
+    if (lower < 0 || upper >= T.n_energy) return false;
+    const R* X = D + T.x;
+    const R* Y = D + T.y;
+    const R* A = D + T.a;
+    const R* B = D + T.b;
+    const int* rs = t.rows + T.row_start;
+    R xl = rita_x_from_y(X, Y, A, B, rs[lower], rs[lower + 1], y);
+    R xu = rita_x_from_y(X, Y, A, B, rs[upper], rs[upper + 1], y);
+    const R* LE = D + T.log_energy;
+    R ll = log_(xl + R(1));
+    mu = exp_(ll + (log_(xu + R(1)) - ll) * (log_(E) - LE[lower]) / (LE[upper] - LE[lower])) - R(1);
+    return true;
+}
+
+// -------------------------------------------------------------------- tally specs ---
+struct DevTally {
+    int kind, nu, nv, reserved;
+    double a[3], b[3], c[3];
+    double radius;
+    double norm[3];      // plane normal used for the entrance cosine
+    double e1e1, e2e2;   // rectangle basis dot products
+    unsigned long long* acc;
+};
+
+// fixed-point scales of the mixed path (per eV, per eV^2, per unit cosine)
+constexpr double kFxEnergy = 4096.0;
+constexpr double kFxEnergy2 = 1.0 / 16.0;
+constexpr double kFxCosine = 1073741824.0;
+
+// Scatter class: 0 primary, 1 single coherent, 2 single incoherent, 3 multiple.
+MIDSX_HD int scatter_class(int n_coh, int n_incoh) {
+    int total = n_coh + n_incoh;
+    if (total > 1) return 3;
+    if (n_coh == 1) return 1;
+    if (n_incoh == 1) return 2;
+    return 0;
+}
+
+}  // namespace midsx

@@ -1,0 +1,139 @@
+// lookup.h - table lookups of the transport path, shared by the CUDA kernels and the
+// host-side evaluator (midsx_tables_eval).  Each function restates one reference lookup:
+//
+//   LogLogLinear::operator()     src/MIDSX/Core/interpolators.cpp:37-76
+//   LogLogSpline::operator()     src/MIDSX/Core/interpolators.cpp:14-31 (Eigen Spline:
+//                                span search and basis functions of Piegl & Tiller,
+//                                "The NURBS Book", algorithms A2.1 and A2.2)
+//   ContinuousInversion::sample  src/MIDSX/Core/probability_dist.cpp:73-119
+//
+// Index searches compare raw energies against raw node arrays.  The reference compares
+// log10 values; log10 is monotone, so the index is the same except where a query lies
+// within rounding of a node, and the raw comparison makes the index a pure function of
+// the stored tables (the CPU oracle and the device agree bit for bit).
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define MIDSX_HD __host__ __device__ __forceinline__
+#else
+#define MIDSX_HD inline
+#include <cmath>
+#endif
+
+namespace midsx {
+
+// First index i in [lo, hi) with a[i] > q (std::upper_bound), hi if none.
+template <typename R>
+MIDSX_HD int upper_index(const R* a, int lo, int hi, R q) {
+    int n = hi - lo;
+    while (n > 0) {
+        int half = n >> 1;
+        if (!(q < a[lo + half])) {  // a[mid] <= q
+            lo += half + 1;
+            n -= half + 1;
+        } else {
+            n = half;
+        }
+    }
+    return lo;
+}
+
+// First index i in [lo, hi) with a[i] >= q (std::lower_bound), hi if none.
+template <typename R>
+MIDSX_HD int lower_index(const R* a, int lo, int hi, R q) {
+    int n = hi - lo;
+    while (n > 0) {
+        int half = n >> 1;
+        if (a[lo + half] < q) {
+            lo += half + 1;
+            n -= half + 1;
+        } else {
+            n = half;
+        }
+    }
+    return lo;
+}
+
+MIDSX_HD double exp10_(double y) { return pow(10.0, y); }
+MIDSX_HD float exp10_(float y) { return powf(10.0f, y); }
+MIDSX_HD double log10_(double y) { return log10(y); }
+MIDSX_HD float log10_(float y) { return log10f(y); }
+MIDSX_HD double log_(double y) { return log(y); }
+MIDSX_HD float log_(float y) { return logf(y); }
+MIDSX_HD double exp_(double y) { return exp(y); }
+MIDSX_HD float exp_(float y) { return expf(y); }
+MIDSX_HD double sqrt_(double y) { return sqrt(y); }
+MIDSX_HD float sqrt_(float y) { return sqrtf(y); }
+
+// Interval index of a LogLogLinear table: 0 = below/at first node (clamp), n = at/above the
+// last node (clamp), else the std::upper_bound position (1..n-1).
+template <typename R>
+MIDSX_HD int lin_index(const R* x, int n, R q) {
+    if (q <= x[0]) return 0;
+    if (q >= x[n - 1]) return n;
+    return upper_index(x, 0, n, q);
+}
+
+template <typename R>
+MIDSX_HD R lin_eval_at(const R* lx, const R* ly, int n, int idx, R q) {
+    if (idx == 0) return exp10_(ly[0]);
+    if (idx >= n) return exp10_(ly[n - 1]);
+    R lq = log10_(q);
+    R x1 = lx[idx - 1], x2 = lx[idx];
+    R y1 = ly[idx - 1], y2 = ly[idx];
+    R slope = (y2 - y1) / (x2 - x1);
+    return exp10_(y1 + slope * (lq - x1));
+}
+
+template <typename R>
+MIDSX_HD R lin_eval(const R* x, const R* lx, const R* ly, int n, R q) {
+    return lin_eval_at(lx, ly, n, lin_index(x, n, q), q);
+}
+
+// Knot span of a B-spline (NURBS Book A2.1 with clamping as in Eigen's Spline::Span):
+// degree if q <= first knot, else upper_bound over knots[degree-1, n_knots-degree-1) - 1.
+template <typename R>
+MIDSX_HD int spline_span(const R* knot_e, int n_ctrl, int degree, R e) {
+    int n_knots = n_ctrl + degree + 1;
+    if (e <= knot_e[0]) return degree;
+    return upper_index(knot_e, degree - 1, n_knots - degree - 1, e) - 1;
+}
+
+template <typename R>
+MIDSX_HD R spline_eval_at(const R* knot_u, const R* ctrl, int degree, int span, R lx_min,
+                          R lx_max, R e) {
+    R u = (log10_(e) - lx_min) / (lx_max - lx_min);
+    R N[4], left[4], right[4];
+    N[0] = R(1);
+    for (int j = 1; j <= degree; ++j) {
+        left[j] = u - knot_u[span + 1 - j];
+        right[j] = knot_u[span + j] - u;
+        R saved = R(0);
+        for (int r = 0; r < j; ++r) {
+            R temp = N[r] / (right[r + 1] + left[j - r]);
+            N[r] = saved + right[r + 1] * temp;
+            saved = left[j - r] * temp;
+        }
+        N[j] = saved;
+    }
+    R v = R(0);
+    for (int i = 0; i <= degree; ++i) v += ctrl[span - degree + i] * N[i];
+    return exp10_(v);
+}
+
+// RITA inverse of one energy row: x(y) from the rational interpolation (PENELOPE eq. 1.54
+// as coded in getXFromY).  rows [r0, r1) hold x, y, a, b.
+template <typename R>
+MIDSX_HD R rita_x_from_y(const R* X, const R* Y, const R* A, const R* B, int r0, int r1, R y) {
+    int j = lower_index(Y, r0, r1, y) - 1;  // findIndexOfNextSmallestValue
+    if (j == r1 - 1) return R(1);           // y above the last CDF value: x_max
+    if (j < r0) return R(-1);               // y below the first: x_min
+    R yi = Y[j], yi1 = Y[j + 1], xi = X[j], xi1 = X[j + 1];
+    R a = A[j], b = B[j];
+    R nu = y - yi;
+    R delta = yi1 - yi;
+    return xi + (R(1) + a + b) * delta * nu / (delta * delta + a * delta * nu + b * nu * nu) * (xi1 - xi);
+}
+
+}  // namespace midsx

@@ -1,0 +1,137 @@
+"""CPU oracle of the transport path - TEST INFRASTRUCTURE ONLY.
+
+A C++/OpenMP restatement of MIDSX's reference transport loop (oracle/oracle.cpp), used by
+tests/, __graft_entry__.smoke() and the CPU legs of bench.py as the checker and the timed
+CPU baseline.  Nothing in midsx_gb300/ imports this package.
+
+Parity is pinned by the reference's own fixtures where they exist (tests/golden/) and by
+the physics checks in tests/; see oracle.cpp for the deviations forced by testing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from midsx_gb300 import native as N
+from midsx_gb300.api import geometry_spec, source_spec, tally_specs
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+RNG_PHILOX, RNG_MT19937 = 0, 1
+
+PD = C.POINTER(C.c_double)
+
+
+class OracleResult(C.Structure):
+    _fields_ = [("dose_sum", PD), ("dose_sumsq", PD), ("dose_count", PD), ("scalar", PD),
+                ("binned_energy", PD), ("binned_count", PD), ("history_deposit", PD),
+                ("stats", N.RunStats), ("run_time", C.c_double)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError("oracle not built; run midsx_gb300.build.build()")
+        lib = C.CDLL(LIB)
+        lib.oracle_run.restype = C.c_int
+        lib.oracle_run.argtypes = [C.POINTER(N.TableBlob), C.POINTER(N.GeometrySpec), C.c_void_p,
+                                   C.POINTER(N.SourceSpec), C.POINTER(N.TallySpec), C.c_int, C.c_uint64,
+                                   C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.POINTER(OracleResult)]
+        lib.oracle_sample.restype = C.c_int
+        lib.oracle_sample.argtypes = [C.POINTER(N.TableBlob), C.c_int, C.c_int, C.c_double, C.c_uint64,
+                                      C.c_uint64, C.c_int64, C.c_int, PD, PD]
+        lib.oracle_table_index.restype = C.c_int
+        lib.oracle_table_index.argtypes = [C.POINTER(N.TableBlob), C.c_int, PD, C.c_int64,
+                                           C.POINTER(C.c_int64)]
+        lib.oracle_philox.restype = None
+        lib.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        _lib = lib
+    return _lib
+
+
+def run(blob, domain, spacing, origin, ids, background_id, source, specs=(), n=1000, seed=1, first=0,
+        rng=RNG_PHILOX, threads=0, max_steps=0, max_trials=0, dose=True, history=False):
+    """blob: midsx_gb300.TableBlob; ids shaped (nz, ny, nx); source: dict(position, direction,
+    energy|spectrum) as for midsx_gb300.source_spec; specs: tally dicts."""
+    lib = load()
+    ids = np.ascontiguousarray(ids, dtype=np.uint8)
+    nz, ny, nx = ids.shape
+    g = geometry_spec(domain, spacing, origin, (nx, ny, nz), background_id)
+    s = source_spec(**source)
+    arr = tally_specs(list(specs))
+    res = OracleResult()
+    keep = {}
+    nvox = ids.size
+    if dose:
+        for k in ("dose_sum", "dose_sumsq", "dose_count"):
+            keep[k] = np.zeros(nvox)
+            setattr(res, k, N.dptr(keep[k]))
+    n_scalar = len(specs)
+    keep["scalar"] = np.zeros(max(1, n_scalar) * N.SCALAR_SLOTS)
+    res.scalar = N.dptr(keep["scalar"])
+    nb = sum(d["nu"] * d["nv"] * 4 for d in specs if d["kind"] == "binned")
+    keep["binned_energy"] = np.zeros(max(1, nb))
+    keep["binned_count"] = np.zeros(max(1, nb))
+    res.binned_energy = N.dptr(keep["binned_energy"])
+    res.binned_count = N.dptr(keep["binned_count"])
+    if history:
+        keep["history_deposit"] = np.zeros(int(n))
+        res.history_deposit = N.dptr(keep["history_deposit"])
+    rc = lib.oracle_run(blob.ptr, C.byref(g), ids.ctypes.data, C.byref(s), arr, len(specs), int(seed), int(first),
+                        int(n), int(rng), int(threads), int(max_steps), int(max_trials), C.byref(res))
+    if rc != 0:
+        raise RuntimeError("oracle_run failed with code %d" % rc)
+    out = {"stats": res.stats.as_dict(), "run_time": res.run_time}
+    if dose:
+        out["dose"] = {"sum": keep["dose_sum"].reshape(ids.shape), "sumsq": keep["dose_sumsq"].reshape(ids.shape),
+                       "count": keep["dose_count"].reshape(ids.shape)}
+    out["scalar"] = [keep["scalar"][i * N.SCALAR_SLOTS:(i + 1) * N.SCALAR_SLOTS] for i in range(n_scalar)]
+    binned, off = [], 0
+    for d in specs:
+        if d["kind"] == "binned":
+            k = d["nu"] * d["nv"] * 4
+            binned.append((keep["binned_energy"][off:off + k].reshape(d["nv"], d["nu"], 4),
+                           keep["binned_count"][off:off + k].reshape(d["nv"], d["nu"], 4)))
+            off += k
+        else:
+            binned.append(None)
+    out["binned"] = binned
+    if history:
+        out["history_deposit"] = keep["history_deposit"]
+    return out
+
+
+def sample(blob, kind, material, energy, n, seed, first=0, rng=RNG_PHILOX):
+    lib = load()
+    k = {"rayleigh": 0, "compton": 1, "freepath": 2}[kind]
+    o0 = np.empty(int(n))
+    o1 = np.empty(int(n))
+    rc = lib.oracle_sample(blob.ptr, k, int(material), float(energy), int(seed), int(first), int(n), int(rng),
+                           N.dptr(o0), N.dptr(o1))
+    if rc != 0:
+        raise RuntimeError("oracle_sample failed")
+    return (o0, o1) if k == 1 else o0
+
+
+def table_index(blob, material, energies):
+    lib = load()
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    idx = np.empty(6 * e.size, dtype=np.int64)
+    rc = lib.oracle_table_index(blob.ptr, int(material), N.dptr(e), e.size, idx.ctypes.data_as(C.POINTER(C.c_int64)))
+    if rc != 0:
+        raise RuntimeError("oracle_table_index failed")
+    return idx.reshape(e.size, 6)
+
+
+def philox(ctr, key):
+    lib = load()
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib.oracle_philox(c, k, o)
+    return list(o)
