@@ -228,7 +228,7 @@ midsx_status midsx_gpu_tallies_reset(midsx_tallies_h t, void* stream);
 
 typedef struct midsx_run_config {
     int32_t precision;           /* midsx_precision */
-    int32_t max_steps;           /* per-history step cap (0 = 1000000) */
+    int32_t max_steps;           /* per-history step cap (0 = 100000) */
     int32_t max_compton_trials;  /* Kahn/S(x) rejection cap (0 = 100000) */
     int32_t block_size;          /* 0 = tuned default */
     int32_t blocks_per_sm;       /* 0 = tuned default */

@@ -1022,7 +1022,7 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
     P.seed = cfg->seed;
     P.first = cfg->first_history;
     P.n = cfg->n_histories;
-    P.max_steps = cfg->max_steps > 0 ? cfg->max_steps : 1000000;
+    P.max_steps = cfg->max_steps > 0 ? cfg->max_steps : 100000;
     P.max_trials = cfg->max_compton_trials > 0 ? cfg->max_compton_trials : 100000;
     P.trace = trace;
     const bool mixed = cfg->precision == MIDSX_PREC_MIXED;

@@ -793,7 +793,7 @@ int oracle_run(const midsx_table_blob* blob, const midsx_geometry_spec* geom, co
     }
     if (out->history_deposit)
         for (uint64_t i = 0; i < n; ++i) out->history_deposit[i] = 0;
-    const int steps_cap = max_steps > 0 ? max_steps : 1000000;
+    const int steps_cap = max_steps > 0 ? max_steps : 100000;
     int progress = 0;
     auto t0 = std::chrono::steady_clock::now();
 #pragma omp parallel num_threads(n_threads)
