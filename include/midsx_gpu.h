@@ -117,6 +117,17 @@ void midsx_tables_free(midsx_table_blob* blob);
 midsx_status midsx_catalog_id(const char* data_dir, const char* name, int32_t* id_out);
 midsx_status midsx_catalog_name(const char* data_dir, int32_t id, char* name_out, int32_t cap);
 
+/* Composition of catalogue material `id` (MaterialProperties, src/MIDSX/Core/
+ * material_properties.cpp:10-77): density (g/cm3) and up to `cap` (Z, weight fraction,
+ * atomic weight g/mol) entries; *n receives the number of elements. */
+midsx_status midsx_catalog_material(const char* data_dir, int32_t id, double* density, int32_t* n,
+                                    int32_t* z, double* weight, double* atomic_weight, int32_t cap);
+
+/* Rayleigh cosine of material `material` at energy E for the uniform y by the RITA inverse
+ * of the built tables (ContinuousInversion::sample, src/MIDSX/Core/probability_dist.cpp:73-88). */
+midsx_status midsx_tables_rita(const midsx_table_blob* blob, int32_t material, double energy, double y,
+                               double* mu);
+
 /* Host evaluation of the built tables, for checks and for the C++ API getters
  * (MaterialData::interpolate*, include/MIDSX/Core/material_data.h:95-143).
  * which: 0 total, 1 photo, 2 coherent (spline), 3 incoherent (spline), 4 S(x), 5 F(x),

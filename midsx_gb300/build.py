@@ -51,6 +51,16 @@ def _cuda_lib_dir():
     return os.path.join(root, "lib64")
 
 
+def _have_zlib():
+    """True when zlib's header and linkable library are installed (the C++ API then reads
+    .nii.gz directly)."""
+    import glob
+    header = any(os.path.exists(os.path.join(d, "zlib.h")) for d in ("/usr/include", "/usr/local/include"))
+    lib = bool(glob.glob("/usr/lib*/libz.so") + glob.glob("/usr/lib/*/libz.so") + glob.glob("/lib/*/libz.so") +
+               glob.glob("/usr/local/lib/libz.so"))
+    return header and lib
+
+
 def _deps(path):
     """Sources a translation unit depends on: itself plus every header in csrc/include."""
     deps = [path]
@@ -104,7 +114,8 @@ def build(verbose=False, with_oracle=True):
         obj = os.path.join(OBJDIR, name + ".o")
         core_objs.append(obj)
         if _stale(obj, _deps(src)):
-            jobs.append((["g++"] + CXX_FLAGS + ["-c", src, "-o", obj], obj))
+            jobs.append((["g++"] + CXX_FLAGS + ([] if _have_zlib() else ["-DMIDSX_NO_ZLIB"]) +
+                         ["-c", src, "-o", obj], obj))
     oracle_src = os.path.join(ORACLE, "oracle.cpp")
     if with_oracle and _stale(LIB_ORACLE, [oracle_src, os.path.join(INCLUDE, "midsx_gpu.h")]):
         jobs.append((["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-I", INCLUDE,
@@ -120,11 +131,24 @@ def build(verbose=False, with_oracle=True):
                      ["-L" + cudalib, "-lcudart_static", "-ldl", "-lpthread", "-lrt"], LIB_MAIN))
     if core_objs and (_stale(LIB_CORE, core_objs) or _stale(LIB_CORE, [LIB_MAIN])):
         link.append((["g++", "-shared", "-fopenmp", "-o", LIB_CORE] + core_objs +
-                     ["-L" + LIBDIR, "-lmidsx_gb300", "-Wl,-rpath,$ORIGIN"], LIB_CORE))
+                     ["-L" + LIBDIR, "-lmidsx_gb300", "-Wl,-rpath,$ORIGIN", "-ldl"] +
+                     (["-lz"] if _have_zlib() else []), LIB_CORE))
     for cmd, target in link:
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         _run_parallel([(cmd, target)])
+    # reference-style C++ programs on the C++ API
+    exdir = os.path.join(PKG, "examples")
+    jobs = []
+    for f in sorted(os.listdir(exdir)) if os.path.isdir(exdir) else []:
+        if not f.endswith(".cpp"):
+            continue
+        exe = os.path.join(LIBDIR, "midsx_example_" + f[:-4])
+        src = os.path.join(exdir, f)
+        if _stale(exe, _deps(src) + [LIB_CORE]):
+            jobs.append((["g++", "-O2", "-std=c++17", "-I", INCLUDE, src, "-o", exe, "-L" + LIBDIR, "-lmidsx_core",
+                          "-lmidsx_gb300", "-Wl,-rpath," + LIBDIR], exe))
+    _run_parallel(jobs)
     return LIB_MAIN
 
 

@@ -637,6 +637,9 @@ midsx_table_blob* build_blob(const std::string& dir, const int32_t* ids, int n, 
     return blob;
 }
 
+std::shared_ptr<DataLibrary> load_library_public(const std::string& dir) { return load_library(dir); }
+const MaterialDef* find_material_public(const DataLibrary& lib, int id) { return find_material(lib, id); }
+
 int catalog_id(const std::string& dir, const std::string& name) {
     auto lib = load_library(dir);
     for (auto& m : lib->materials)
@@ -716,6 +719,43 @@ extern "C" midsx_status midsx_catalog_name(const char* data_dir, int32_t id, cha
         std::snprintf(name_out, size_t(cap), "%s", s.c_str());
         return MIDSX_OK;
     })
+}
+
+extern "C" midsx_status midsx_catalog_material(const char* data_dir, int32_t id, double* density, int32_t* n,
+                                               int32_t* z, double* weight, double* atomic_weight, int32_t cap) {
+    if (!data_dir || !density || !n) return MIDSX_INVALID_ARG;
+    MIDSX_GUARD({
+        auto lib = midsx::load_library_public(data_dir);
+        const auto* m = midsx::find_material_public(*lib, id);
+        if (!m) {
+            set_last_error("unknown material id " + std::to_string(id));
+            return MIDSX_NOT_FOUND;
+        }
+        *density = m->density;
+        *n = int32_t(m->comp.size());
+        for (int32_t i = 0; i < *n && i < cap; ++i) {
+            if (z) z[i] = m->comp[size_t(i)].first;
+            if (weight) weight[i] = m->comp[size_t(i)].second;
+            if (atomic_weight) atomic_weight[i] = lib->atomic_weight.at(m->comp[size_t(i)].first);
+        }
+        return MIDSX_OK;
+    })
+}
+
+extern "C" midsx_status midsx_tables_rita(const midsx_table_blob* blob, int32_t material, double energy, double y,
+                                          double* mu) {
+    if (!blob || !mu || material < 0 || material >= blob->n_materials) return MIDSX_INVALID_ARG;
+    const midsx_rita_table& r = blob->mat[material].rita;
+    const double* D = blob->data;
+    const int64_t* rows = blob->idata + r.row_start;
+    int lower = midsx::lower_index(D + r.energy, 0, r.n_energy, energy) - 1;
+    if (lower < 0 || lower + 1 >= r.n_energy) return MIDSX_TABLE_RANGE;
+    const double *X = D + r.x, *Y = D + r.y, *A = D + r.a, *B = D + r.b, *LE = D + r.log_energy;
+    double xl = midsx::rita_x_from_y(X, Y, A, B, int(rows[lower]), int(rows[lower + 1]), y);
+    double xu = midsx::rita_x_from_y(X, Y, A, B, int(rows[lower + 1]), int(rows[lower + 2]), y);
+    double ll = std::log(xl + 1);
+    *mu = std::exp(ll + (std::log(xu + 1) - ll) * (std::log(energy) - LE[lower]) / (LE[lower + 1] - LE[lower])) - 1;
+    return MIDSX_OK;
 }
 
 extern "C" midsx_status midsx_tables_eval(const midsx_table_blob* blob, int32_t material,
