@@ -243,7 +243,8 @@ typedef struct midsx_run_config {
     int32_t max_compton_trials;  /* Kahn/S(x) rejection cap (0 = 100000) */
     int32_t block_size;          /* 0 = tuned default */
     int32_t blocks_per_sm;       /* 0 = tuned default */
-    int32_t reserved;
+    int32_t regroup;             /* lanes of a warp parked on a real collision before the warp runs
+                                    its collisions together (1 = at once; 0 = tuned default) */
     uint64_t seed;
     uint64_t first_history;      /* history ids [first, first + n) select Philox streams */
     uint64_t n_histories;

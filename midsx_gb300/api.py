@@ -292,8 +292,9 @@ class Tallies:
 PRECISIONS = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}
 
 
-def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0):
+def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0, regroup=0):
     c = N.RunConfig()
+    c.regroup = int(regroup)
     c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     c.n_histories = int(n)
     c.seed = int(seed)

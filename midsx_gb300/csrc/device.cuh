@@ -104,6 +104,18 @@ struct HistoryRng {
         ++n;
         return r;
     }
+    // The two draws of one Woodcock step (free path, delta test) come from one Philox block:
+    // the counter is first rounded up to an even draw index, so a step always costs exactly
+    // one block.  first = draw 2k, second = draw 2k + 1; afterwards n = 2k + 2.
+    MIDSX_HD void next_pair64(uint64_t& first, uint64_t& second) {
+        uint32_t blk = (n + 1u) >> 1;
+        Philox4 w = philox4x32_10(blk, h0, h1, 0u, k0, k1);
+        first = (uint64_t(w.v[0]) << 32) | w.v[1];
+        second = (uint64_t(w.v[2]) << 32) | w.v[3];
+        b0 = w.v[2];
+        b1 = w.v[3];
+        n = 2u * blk + 2u;
+    }
 };
 
 // Uniform in (0, 1].

@@ -1,11 +1,12 @@
 // transport.cu - GB300 (sm_103a) kernels of MIDSX's photon-history loop and their C ABI.
 //
-// One CUDA thread transports one history at a time (grid-stride over history ids); the
-// history's state (position, direction, energy, scatter counts, Philox counter) lives in
-// registers.  Per history the loop is the reference's Woodcock step
-// (src/MIDSX/Core/physics_engine.cpp:28-79): majorant free path, domain test, voxel
-// material fetch, delta test, interaction.  Tallies are scored per step instead of
-// after the history (processTallies, physics_engine.cpp:192-210); all tallies are sums,
+// Each lane of a warp owns one history at a time (history ids strided by the number of
+// threads) and starts its next history as soon as the current one ends; the history's
+// state (position, direction, energy, scatter counts, Philox counter) lives in registers.
+// A loop iteration is the reference's Woodcock step (src/MIDSX/Core/physics_engine.cpp:28-79):
+// majorant free path, domain test, voxel material fetch, delta test; real collisions are
+// parked and run by the warp together (kernel_body.cuh).  Tallies are scored per step instead
+// of after the history (processTallies, physics_engine.cpp:192-210); all tallies are sums,
 // so the order does not change the result.
 //
 // Energy-dependent table values (majorant and every material's total cross section)
@@ -66,6 +67,7 @@ struct RunParams {
     unsigned long long* stats;
     uint64_t seed, first, n;
     int max_steps, max_trials;
+    int regroup;    // lanes of a warp that wait for a real collision before the warp runs them
     double* trace;  // optional: energy deposited in grid voxels per history
 };
 
@@ -131,7 +133,7 @@ __device__ __forceinline__ void vec_cosine(unsigned long long* acc, int q, int c
 // cls1: class of final_photon (post-interaction counts if the step interacted, else
 // a default Photon = primary), used by volume quantities.
 template <typename R, bool MX>
-__device__ void score_tallies(const RunParams& P, const V3<R>& p0, const V3<R>& d, R s, R E, int cls0,
+__device__ __noinline__ void score_tallies(const RunParams& P, const V3<R>& p0, const V3<R>& d, R s, R E, int cls0,
                               int cls1, bool interact, R dep, uint32_t& words) {
     for (int ti = 0; ti < P.n_tallies; ++ti) {
         const DevTally& T = P.tallies[ti];
@@ -271,223 +273,8 @@ __device__ void sample_source(const DevSource& S, HistoryRng& rng, V3<R>& pos, V
     }
 }
 
-// ---------------------------------------------------------------- per-energy cache ---
-template <typename R>
-__device__ __forceinline__ R refresh_energy(const RunParams& P, R E, R* thr, R* mu, int stride) {
-    R mu_max = lin_lookup<R>(P.T, P.T.majorant, E);
-    for (int m = 0; m < P.T.n_materials; ++m) {
-        R mm = lin_lookup<R>(P.T, P.T.mat[m].total, E);
-        mu[m * stride] = mm;
-        thr[m * stride] = R(1) - mm / mu_max;  // p_delta of isDeltaScatter
-    }
-    return mu_max;
-}
-
 // -------------------------------------------------------------------- the kernel ---
-template <typename R>
-__global__ void __launch_bounds__(256) transport_kernel(const RunParams P) {
-    constexpr bool MX = sizeof(R) == 4;
-    extern __shared__ unsigned char smem_raw[];
-    R* cache = reinterpret_cast<R*>(smem_raw);
-    const int stride = blockDim.x;
-    const int M = P.T.n_materials;
-    R* thr = cache + threadIdx.x;
-    R* mucache = cache + M * stride + threadIdx.x;
-
-    // per-thread statistics, flushed once at the end
-    unsigned long long st_hist = 0, st_steps = 0, st_fetch = 0, st_photo = 0, st_coh = 0, st_incoh = 0;
-    unsigned long long st_trials = 0, st_stepcap = 0, st_trialcap = 0, st_edge = 0, st_words = 0;
-    unsigned long long st_src = 0, st_dgrid = 0, st_dbg = 0, st_esc = 0, st_range = 0, st_nonfinite = 0;
-
-    const R alpha = R(P.T.alpha);
-    const V3<R> dom = {R(P.G.domain[0]), R(P.G.domain[1]), R(P.G.domain[2])};
-    const V3<R> org = {R(P.G.origin[0]), R(P.G.origin[1]), R(P.G.origin[2])};
-    const V3<R> ext = {R(P.G.ext[0]), R(P.G.ext[1]), R(P.G.ext[2])};
-    const V3<R> spc = {R(P.G.spacing[0]), R(P.G.spacing[1]), R(P.G.spacing[2])};
-    const int nx = P.G.dims[0], ny = P.G.dims[1], nz = P.G.dims[2];
-    const bool have_tallies = P.n_tallies > 0;
-
-    const uint64_t total_threads = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t h = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; h < P.n; h += total_threads) {
-        HistoryRng rng;
-        rng.init(P.seed, P.first + h);
-        V3<R> pos, dir;
-        R E;
-        sample_source<R>(P.S, rng, pos, dir, E);
-        ++st_hist;
-        st_src += (unsigned long long)llrint(double(E) * kFxStat);
-        int n_coh = 0, n_incoh = 0;
-        double hist_dep = 0.0;
-        R mu_max = refresh_energy<R>(P, E, thr, mucache, stride);
-        for (int step = 0;; ++step) {
-            if (step >= P.max_steps) {
-                ++st_stepcap;
-                break;
-            }
-            ++st_steps;
-            // getFreePath + move
-            R s = -log_(uniform<R>(rng)) / mu_max;
-            const V3<R> p0 = pos;
-            pos = {pos.x + s * dir.x, pos.y + s * dir.y, pos.z + s * dir.z};
-            const int cls0 = scatter_class(n_coh, n_incoh);
-            // isInComputationalDomain (NaN positions count as outside)
-            if (!(pos.x >= R(0) && pos.x <= dom.x && pos.y >= R(0) && pos.y <= dom.y && pos.z >= R(0) &&
-                  pos.z <= dom.z)) {
-                if (have_tallies) {
-                    uint32_t w = 0;
-                    score_tallies<R, MX>(P, p0, dir, s, E, cls0, 0, false, R(0), w);
-                    st_words += w;
-                }
-                st_esc += (unsigned long long)llrint(double(E) * kFxStat);
-                break;
-            }
-            // ComputationalDomain::getVoxel: grid voxel (inclusive bounds) or background
-            V3<R> q = {pos.x - org.x, pos.y - org.y, pos.z - org.z};
-            int mat;
-            long long vox = -1;
-            if (q.x >= R(0) && q.x <= ext.x && q.y >= R(0) && q.y <= ext.y && q.z >= R(0) && q.z <= ext.z) {
-                int ix = int(q.x / spc.x), iy = int(q.y / spc.y), iz = int(q.z / spc.z);
-                if (ix >= nx || iy >= ny || iz >= nz) {
-                    ++st_edge;  // the reference's vector::at would throw here
-                    ix = min(ix, nx - 1);
-                    iy = min(iy, ny - 1);
-                    iz = min(iz, nz - 1);
-                }
-                vox = (long long)ix + (long long)iy * nx + (long long)iz * nx * ny;
-                mat = __ldg(P.G.ids + vox);
-                ++st_fetch;
-            } else {
-                mat = P.G.background;
-            }
-            // isDeltaScatter
-            R u2 = uniform<R>(rng);
-            if (u2 < thr[mat * stride]) {
-                if (have_tallies) {
-                    uint32_t w = 0;
-                    score_tallies<R, MX>(P, p0, dir, s, E, cls0, 0, false, R(0), w);
-                    st_words += w;
-                }
-                continue;
-            }
-            // setInteractionType
-            const DevMaterial& Mt = P.T.mat[mat];
-            const R mu_tot = mucache[mat * stride];
-            R p_coh = spline_lookup<R>(P.T, Mt.coh, E) / mu_tot;
-            R p_incoh = spline_lookup<R>(P.T, Mt.incoh, E) / mu_tot;
-            R u3 = uniform<R>(rng);
-            const R E0 = E;
-            const V3<R> d0 = dir;
-            R dep = R(0);
-            bool terminated = false;
-            bool energy_changed = false;
-            if (u3 < p_coh) {
-                // CoherentScattering::interact
-                ++n_coh;
-                ++st_coh;
-                R mu;
-                if (!rita_sample<R>(P.T, Mt.rita, E, uniform<R>(rng), mu)) {
-                    ++st_range;
-                    break;
-                }
-                R theta = acos_(mu);
-                R phi = R(2 * kPi) * uniform<R>(rng);
-                dir = rotate_direction(dir, theta, phi);
-            } else if (u3 < p_coh + p_incoh) {
-                // IncoherentScattering::interact (Kahn + S(x) rejection)
-                ++n_incoh;
-                ++st_incoh;
-                const R k = E / R(kMec2);
-                const R r1p = (R(1) + R(2) * k) / (R(9) + R(2) * k);
-                const R s_max = lin_lookup<R>(P.T, Mt.sfunc, alpha * k * sqrt_(R(2)));
-                R mu = R(1), kp = k;
-                bool accepted = false;
-                for (int trial = 0; trial < P.max_trials; ++trial) {
-                    ++st_trials;
-                    R r1 = uniform<R>(rng), r2 = uniform<R>(rng), r3 = uniform<R>(rng);
-                    R chi;
-                    if (r1 <= r1p) {
-                        chi = R(1) + R(2) * k * r2;
-                        if (!(r3 <= R(4) * (R(1) / chi - R(1) / (chi * chi)))) continue;
-                    } else {
-                        chi = (R(1) + R(2) * k) / (R(1) + R(2) * k * r2);
-                        R tt = R(1) / k - chi / k + R(1);
-                        if (!(R(2) * r3 <= tt * tt + R(1) / chi)) continue;
-                    }
-                    kp = k / chi;
-                    mu = R(1) + R(1) / k - R(1) / kp;
-                    R x = alpha * k * sqrt_(R(1) - mu);
-                    R accept = lin_lookup<R>(P.T, Mt.sfunc, x) / s_max;
-                    if (uniform<R>(rng) <= accept) {
-                        accepted = true;
-                        break;
-                    }
-                }
-                if (!accepted) {
-                    ++st_trialcap;
-                    break;
-                }
-                R theta = acos_(mu);
-                R phi = R(2 * kPi) * uniform<R>(rng);
-                dir = rotate_direction(dir, theta, phi);
-                E = kp * R(kMec2);
-                dep = R(kMec2) * (k - kp);
-                energy_changed = true;
-            } else {
-                // PhotoelectricEffect::interact
-                ++st_photo;
-                dep = E;
-                terminated = true;
-            }
-            const int cls1 = scatter_class(n_coh, n_incoh);
-            if (have_tallies) {
-                uint32_t w = 0;
-                score_tallies<R, MX>(P, p0, d0, s, E0, cls0, cls1, true, dep, w);
-                st_words += w;
-            }
-            if (dep != R(0)) {
-                unsigned long long fx = (unsigned long long)llrint(double(dep) * kFxStat);
-                if (vox >= 0) {
-                    st_dgrid += fx;
-                    hist_dep += double(dep);
-                    if (P.dose_stride) {
-                        unsigned long long* rec = P.dose + size_t(vox) * P.dose_stride;
-                        Acc<MX>::energy(rec, double(dep));
-                        ++st_words;  // one 32-byte voxel record
-                        if (P.dose_stride > 1) {
-                            Acc<MX>::energy2(rec + 1, double(dep));
-                            count1(rec + 2);
-                        }
-                    }
-                } else {
-                    st_dbg += fx;
-                }
-            }
-            if (terminated) break;
-            if (!(fabs_(dir.x) <= R(2) && fabs_(dir.y) <= R(2) && fabs_(dir.z) <= R(2))) {
-                // a NaN direction (RITA rows below ~400 eV are NaN, as in the reference);
-                // the reference's next step would leave the domain: retire the history.
-                ++st_nonfinite;
-                st_esc += (unsigned long long)llrint(double(E) * kFxStat);
-                break;
-            }
-            if (energy_changed) mu_max = refresh_energy<R>(P, E, thr, mucache, stride);
-        }
-        if (P.trace) P.trace[h] = hist_dep;
-    }
-    // flush statistics: warp reduction, then one atomic per warp and counter
-    unsigned long long v[kStCount] = {st_hist, st_steps, st_fetch, st_photo, st_coh, st_incoh,
-                                      st_trials, st_stepcap, st_trialcap, st_edge, st_words, st_src,
-                                      st_dgrid, st_dbg, st_esc, st_range, st_nonfinite};
-    const unsigned lane = threadIdx.x & 31u;
-#pragma unroll
-    for (int i = 0; i < kStCount; ++i) {
-        unsigned long long x = v[i];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0 && x) atomicAdd(P.stats + i, x);
-    }
-}
-
+#include "kernel_body.cuh"
 // ------------------------------------------------------------- diagnostics kernels ---
 template <typename R>
 __global__ void sample_kernel(const DevTables T, int kind, int m, double energy, uint64_t seed, uint64_t first,
@@ -1025,6 +812,7 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
     P.max_steps = cfg->max_steps > 0 ? cfg->max_steps : 100000;
     P.max_trials = cfg->max_compton_trials > 0 ? cfg->max_compton_trials : 100000;
     P.trace = trace;
+    P.regroup = cfg->regroup > 0 ? std::min(cfg->regroup, 32) : 16;
     const bool mixed = cfg->precision == MIDSX_PREC_MIXED;
     int block = cfg->block_size > 0 ? cfg->block_size : 256;
     if (block > 256 || block % 32) {

@@ -76,7 +76,7 @@ class TallySpec(C.Structure):
 class RunConfig(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_steps", C.c_int32),
                 ("max_compton_trials", C.c_int32), ("block_size", C.c_int32),
-                ("blocks_per_sm", C.c_int32), ("reserved", C.c_int32), ("seed", C.c_uint64),
+                ("blocks_per_sm", C.c_int32), ("regroup", C.c_int32), ("seed", C.c_uint64),
                 ("first_history", C.c_uint64), ("n_histories", C.c_uint64)]
 
 

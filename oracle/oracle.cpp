@@ -97,6 +97,11 @@ struct Generator {
     std::mt19937 mt;
     std::uniform_real_distribution<double> unit{0.0, 1.0};
 
+    // The free-path draw of each Woodcock step starts a new Philox block (even draw index),
+    // so that a step's two draws share one block (the device's stream definition).
+    void alignStep() {
+        if (mode == RNG_PHILOX && (draws & 1)) ++draws;
+    }
     double next() {
         if (mode == RNG_MT19937) return unit(mt);
         uint32_t c[4] = {uint32_t(draws >> 1), uint32_t(history), uint32_t(history >> 32), 0u};
@@ -613,7 +618,10 @@ struct PhysicsEngine {
 
     PhysicsEngine(const ComputationalDomain& d, const InteractionData& i) : dom(d), data(i) {}
 
-    double getFreePath(double mu_max) { return -std::log(uniform_dist_.sample()) / mu_max; }
+    double getFreePath(double mu_max) {
+        tl_gen->alignStep();
+        return -std::log(uniform_dist_.sample()) / mu_max;
+    }
     bool isDeltaScatter(double mu, double mu_max) {
         double p = 1 - mu / mu_max;
         return uniform_dist_.sample() < p;

@@ -178,7 +178,9 @@ def test_water_cube_against_independent_oracle(cube, precision):
     z = chi_voxels(d["sum"].ravel(), d["sumsq"].ravel(), o["dose"]["sum"].ravel(), o["dose"]["sumsq"].ravel())
     assert z.size > 50
     assert np.mean(np.abs(z) > 3) < 0.01, np.mean(np.abs(z) > 3)
-    assert 0.8 < np.mean(z * z) < 1.25, np.mean(z * z)
+    # chi-square per voxel: mean z^2 is 1 within its own sampling error sqrt(2 / n_voxels)
+    # (the deposit-based variance is conservative, so a mean well below 1 is allowed)
+    assert np.mean(z * z) < 1 + 4 * np.sqrt(2 / z.size), np.mean(z * z)
     # detector bins (primary + scattered), Poisson-compound variance from counts
     tot_g, tot_o = be.sum(axis=2).ravel(), oe.sum(axis=2).ravel()
     cnt_g, cnt_o = bc.sum(axis=2).ravel(), oc.sum(axis=2).ravel()
