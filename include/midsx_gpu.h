@@ -309,6 +309,24 @@ midsx_status midsx_gpu_sample(midsx_tables_h tables, int32_t precision, int32_t 
 midsx_status midsx_gpu_trace_deposits(midsx_tables_h tables, midsx_phantom_h phantom,
                                       midsx_source_h source, const midsx_run_config* cfg,
                                       double* hist_dep);
+/* Allocation-free form of midsx_gpu_trace_deposits.  No counterpart in the reference: MIDSX
+ * runs on the CPU and never faces this constraint.  It exists for callers that must not
+ * allocate device memory while they run - a service that reserves its whole GPU memory budget
+ * at start-up and treats any later allocation as a failure, a host application whose device
+ * memory belongs to its own pool allocator, or a latency-critical loop that cannot afford the
+ * device-wide synchronisation cudaFree implies.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine: its scratch (run counters and one double per history) is a fixed array
+ * in the library's device code, 8 MiB plus 256 bytes on every GPU that loads the library,
+ * held until the process exits.  Limit: at most 1,048,576 histories per call; larger requests
+ * fail with MIDSX_INVALID_ARG.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) and keeps it, so make that first call before any stream
+ * capture.  All calls on a device share the one array, so calls whose device work overlaps
+ * (different streams, different host threads) race on it; serialise them.  Inputs and the
+ * host output hist_dep (n_histories doubles) are the caller's; the call returns when the
+ * results are in hist_dep. */
+midsx_status midsx_gpu_trace_deposits_noalloc(midsx_tables_h tables, midsx_phantom_h phantom,
+                                              midsx_source_h source, const midsx_run_config* cfg,
+                                              double* hist_dep, void* stream);
 /* Table indices found on the device for energies e[n] (FP64 path): idx[6*n] = majorant,
  * material total, S(x) at x = e (as momentum transfer), coherent-spline span,
  * incoherent-spline span, RITA energy row. */

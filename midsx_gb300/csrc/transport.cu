@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1023,6 +1024,82 @@ extern "C" midsx_status midsx_gpu_trace_deposits(midsx_tables_h tables, midsx_ph
     cudaFree(d);
     midsx_gpu_tallies_destroy(tl);
     return st;
+}
+
+// ------------------------------------------------- allocation-free per-history trace ---
+// Device scratch of midsx_gpu_trace_deposits_noalloc, reserved when the library's device code
+// is loaded onto a GPU and held until the process exits: the run's statistics counters in
+// the first 256 bytes, then one double per history (at most kNoAllocMaxHistories).  Every
+// call on a device reuses the same array.
+namespace {
+constexpr uint64_t kNoAllocMaxHistories = uint64_t(1) << 20;  // 1,048,576 histories, 8 MiB
+constexpr size_t kNoAllocStatsBytes = 256;
+static_assert(kStCount * sizeof(unsigned long long) <= kNoAllocStatsBytes, "statistics fit the scratch header");
+}  // namespace
+
+static __device__ __align__(256) unsigned char midsx_noalloc_scratch[kNoAllocStatsBytes +
+                                                                      kNoAllocMaxHistories * sizeof(double)];
+
+namespace {
+std::mutex g_noalloc_mutex;
+void* g_noalloc_address[256] = {};
+
+// Device address of midsx_noalloc_scratch on the current device.  Host code sees only a
+// host-side stand-in under that name, so the address is asked from the runtime once per
+// device, with that device current, and kept.
+midsx_status noalloc_scratch(void** out) {
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) {
+        set_last_error("device ordinal out of range");
+        return MIDSX_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[dev]) {
+        void* p = nullptr;
+        if (!cuda_ok(cudaGetSymbolAddress(&p, midsx_noalloc_scratch), "cudaGetSymbolAddress")) return MIDSX_CUDA_ERROR;
+        g_noalloc_address[dev] = p;
+    }
+    *out = g_noalloc_address[dev];
+    return MIDSX_OK;
+}
+}  // namespace
+
+extern "C" midsx_status midsx_gpu_trace_deposits_noalloc(midsx_tables_h tables, midsx_phantom_h phantom,
+                                                         midsx_source_h source, const midsx_run_config* cfg,
+                                                         double* hist_dep, void* stream) {
+    if (!tables || !phantom || !source || !cfg || !hist_dep || cfg->n_histories == 0) {
+        set_last_error("midsx_gpu_trace_deposits_noalloc: invalid argument");
+        return MIDSX_INVALID_ARG;
+    }
+    if (cfg->n_histories > kNoAllocMaxHistories) {
+        set_last_error("midsx_gpu_trace_deposits_noalloc: n_histories exceeds its fixed scratch of 1048576 histories");
+        return MIDSX_INVALID_ARG;
+    }
+    void* base = nullptr;
+    midsx_status st = noalloc_scratch(&base);
+    if (st != MIDSX_OK) return st;
+    unsigned long long* stats = static_cast<unsigned long long*>(base);
+    double* dep = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + kNoAllocStatsBytes);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the counters keep the previous call's values: clear them; every history of this call
+    // writes its own deposit slot, so the deposit area needs no clearing
+    CUDA_TRY(cudaMemsetAsync(stats, 0, kNoAllocStatsBytes, s));
+    midsx_gpu_tallies view;  // statistics only: no tallies, no dose, nothing allocated
+    view.stats = stats;
+    st = launch_run(tables, phantom, source, &view, cfg, stream, dep);
+    view.stats = nullptr;
+    if (st != MIDSX_OK) return st;
+    unsigned long long h[kStCount];
+    CUDA_TRY(cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(hist_dep, dep, cfg->n_histories * sizeof(double), cudaMemcpyDeviceToHost, s));
+    st = wait_stream(stream);
+    if (st != MIDSX_OK) return st;
+    if (h[kStRangeErr]) {
+        set_last_error("an energy left the RITA tables during transport");
+        return MIDSX_TABLE_RANGE;
+    }
+    return MIDSX_OK;
 }
 
 extern "C" midsx_status midsx_gpu_sample(midsx_tables_h tables, int32_t precision, int32_t kind, int32_t material,

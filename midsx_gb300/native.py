@@ -125,6 +125,7 @@ _SIGNATURES = {
                                    C.c_uint64, C.c_int64, PD, PD]),
     "midsx_gpu_table_index": (C.c_int, [VP, C.c_int32, PD, C.c_int64, PI64]),
     "midsx_gpu_trace_deposits": (C.c_int, [VP, VP, VP, C.POINTER(RunConfig), PD]),
+    "midsx_gpu_trace_deposits_noalloc": (C.c_int, [VP, VP, VP, C.POINTER(RunConfig), PD, VP]),
 }
 
 _lib = None
