@@ -327,9 +327,11 @@ midsx_status midsx_gpu_trace_deposits(midsx_tables_h tables, midsx_phantom_h pha
 midsx_status midsx_gpu_trace_deposits_noalloc(midsx_tables_h tables, midsx_phantom_h phantom,
                                               midsx_source_h source, const midsx_run_config* cfg,
                                               double* hist_dep, void* stream);
-/* Table indices found on the device for energies e[n] (FP64 path): idx[6*n] = majorant,
- * material total, S(x) at x = e (as momentum transfer), coherent-spline span,
- * incoherent-spline span, RITA energy row. */
+/* Table indices found on the device for energies e[n] (FP64 path, the bucketed searches the
+ * transport kernel uses): idx[6*n] = majorant, material total, S(x) at x = e (as momentum
+ * transfer), coherent-spline span, incoherent-spline span, RITA energy row.  An entry is
+ * -1000 where the FP32 path's bucketed search at float(e) differs from a full search of the
+ * FP32 node array (a self-check of the FP32 bucket tables). */
 midsx_status midsx_gpu_table_index(midsx_tables_h tables, int32_t material, const double* e,
                                    int64_t n, int64_t* idx);
 

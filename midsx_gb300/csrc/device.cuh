@@ -207,15 +207,21 @@ MIDSX_HD V3<R> rotate_direction(const V3<R>& v, R theta, R phi) {
 }
 
 // ----------------------------------------------------------------- device tables ---
+// Each searched node array carries two bucket tables (lookup.h, BucketSpec): one for FP64
+// queries against the FP64 nodes (bk_d) and one for FP32 queries against the FP32 nodes
+// (bk_f), offsets into DevTables::bk.  kind 0 = energy (eV), 1 = momentum transfer (1/A).
 struct DevLin {
     int x, lx, ly, n;
+    int bk_d, bk_f, kind;
 };
 struct DevSpline {
     int knot_e, knot_u, ctrl, n_ctrl, degree;
+    int bk_d, bk_f;
     double lx_min, lx_max;
 };
 struct DevRita {
     int energy, log_energy, row_start, x, y, a, b, n_energy;
+    int bk_d, bk_f;
 };
 struct DevMaterial {
     DevLin total, sfunc;
@@ -226,6 +232,8 @@ struct DevTables {
     const double* d;     // FP64 data (blob layout)
     const float* f;      // FP32 copy, same offsets
     const int* rows;     // RITA row starts
+    const int* bk;       // bucket tables of every searched node array
+    BucketSpec bs[2][2];  // [kind][0 = FP64 query, 1 = FP32 query]
     int n_materials;
     double alpha;        // 1/Angstrom per unit k
     double e_max;
@@ -245,16 +253,55 @@ MIDSX_HD const float* tab<float>(const DevTables& t) {
 }
 
 template <typename R>
+MIDSX_HD const int* buckets(const DevTables& t, int bk_d, int bk_f) {
+    return t.bk + (sizeof(R) == 8 ? bk_d : bk_f);
+}
+template <typename R>
+MIDSX_HD const BucketSpec& bspec(const DevTables& t, int kind) {
+    return t.bs[kind][sizeof(R) == 8 ? 0 : 1];
+}
+
+// LogLogLinear interval index with the bucketed search (same result as lin_index).
+template <typename R>
+MIDSX_HD int lin_index_bk(const DevTables& t, const DevLin& L, R q) {
+    const R* x = tab<R>(t) + L.x;
+    if (q <= x[0]) return 0;
+    if (q >= x[L.n - 1]) return L.n;
+    const int* st = buckets<R>(t, L.bk_d, L.bk_f);
+    int b = bucket_of(q, bspec<R>(t, L.kind));
+    return upper_index(x, st[b], st[b + 1], q);
+}
+
+template <typename R>
 MIDSX_HD R lin_lookup(const DevTables& t, const DevLin& L, R q) {
     const R* D = tab<R>(t);
-    return lin_eval(D + L.x, D + L.lx, D + L.ly, L.n, q);
+    return lin_eval_at(D + L.lx, D + L.ly, L.n, lin_index_bk<R>(t, L, q), q);
+}
+
+// Knot span with the bucketed search (same result as spline_span).
+template <typename R>
+MIDSX_HD int spline_span_bk(const DevTables& t, const DevSpline& S, R e) {
+    const R* ke = tab<R>(t) + S.knot_e;
+    if (e <= ke[0]) return S.degree;
+    const int* st = buckets<R>(t, S.bk_d, S.bk_f);
+    int b = bucket_of(e, bspec<R>(t, 0));
+    return upper_index(ke, st[b], st[b + 1], e) - 1;
 }
 
 template <typename R>
 MIDSX_HD R spline_lookup(const DevTables& t, const DevSpline& S, R e) {
     const R* D = tab<R>(t);
-    int span = spline_span(D + S.knot_e, S.n_ctrl, S.degree, e);
+    int span = spline_span_bk<R>(t, S, e);
     return spline_eval_at(D + S.knot_u, D + S.ctrl, S.degree, span, R(S.lx_min), R(S.lx_max), e);
+}
+
+// Lower RITA energy row (lower_bound - 1) with the bucketed search.
+template <typename R>
+MIDSX_HD int rita_row_bk(const DevTables& t, const DevRita& T, R E) {
+    const R* en = tab<R>(t) + T.energy;
+    const int* st = buckets<R>(t, T.bk_d, T.bk_f);
+    int b = bucket_of(E, bspec<R>(t, 0));
+    return lower_index(en, st[b], st[b + 1], E) - 1;
 }
 
 // ContinuousInversion::sample (probability_dist.cpp:73-88).  Returns false if E has no
@@ -262,7 +309,7 @@ MIDSX_HD R spline_lookup(const DevTables& t, const DevSpline& S, R e) {
 template <typename R>
 MIDSX_HD bool rita_sample(const DevTables& t, const DevRita& T, R E, R y, R& mu) {
     const R* D = tab<R>(t);
-    int lower = lower_index(D + T.energy, 0, T.n_energy, E) - 1;
+    int lower = rita_row_bk<R>(t, T, E);
     int upper = lower + 1;
     if (lower < 0 || upper >= T.n_energy) return false;
     const R* X = D + T.x;

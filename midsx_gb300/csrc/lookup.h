@@ -55,6 +55,47 @@ MIDSX_HD int lower_index(const R* a, int lo, int hi, R q) {
     return lo;
 }
 
+// ------------------------------------------------------------ bucketed search ------
+// A node array x[0..n) is paired with a bucket table over the floating-point bit pattern of
+// the query: bucket b holds every query whose top bits (sign, exponent, top K mantissa bits)
+// equal base + b, i.e. an exact binade slice [lo(b), lo(b + 1)).  starts[b] is the search
+// result for lo(b), computed on the host with the same comparison, so for any query in the
+// slice the result lies in [starts[b], starts[b + 1]] and a search over that range gives
+// exactly the full-array answer.  Queries below the first slice use slice 0 (starts[0] is the
+// range start), queries above the last use the last slice (starts[nb] is the range end).
+struct BucketSpec {
+    int kbits;       // mantissa bits per binade slice
+    long long base;  // key of the first slice
+    int nb;          // number of slices
+};
+
+MIDSX_HD long long bucket_key(double q, int kbits) {
+#if defined(__CUDA_ARCH__)
+    unsigned long long bits = (unsigned long long)__double_as_longlong(q);
+#else
+    unsigned long long bits;
+    __builtin_memcpy(&bits, &q, 8);
+#endif
+    return (long long)(bits >> (52 - kbits));
+}
+
+MIDSX_HD long long bucket_key(float q, int kbits) {
+#if defined(__CUDA_ARCH__)
+    unsigned int bits = __float_as_uint(q);
+#else
+    unsigned int bits;
+    __builtin_memcpy(&bits, &q, 4);
+#endif
+    return (long long)(bits >> (23 - kbits));
+}
+
+template <typename R>
+MIDSX_HD int bucket_of(R q, const BucketSpec& s) {
+    long long b = bucket_key(q, s.kbits) - s.base;
+    if (!(q > R(0))) b = 0;  // zero, negative or NaN queries: first slice
+    return b < 0 ? 0 : (b >= s.nb ? s.nb - 1 : int(b));
+}
+
 MIDSX_HD double exp10_(double y) { return pow(10.0, y); }
 MIDSX_HD float exp10_(float y) { return powf(10.0f, y); }
 MIDSX_HD double log10_(double y) { return log10(y); }

@@ -324,14 +324,23 @@ __global__ void index_kernel(const DevTables T, int m, const double* e, int64_t 
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double E = e[i];
-    const double* D = T.d;
     const DevMaterial& Mt = T.mat[m];
-    idx[6 * i + 0] = lin_index(D + T.majorant.x, T.majorant.n, E);
-    idx[6 * i + 1] = lin_index(D + Mt.total.x, Mt.total.n, E);
-    idx[6 * i + 2] = lin_index(D + Mt.sfunc.x, Mt.sfunc.n, E);
-    idx[6 * i + 3] = spline_span(D + Mt.coh.knot_e, Mt.coh.n_ctrl, Mt.coh.degree, E);
-    idx[6 * i + 4] = spline_span(D + Mt.incoh.knot_e, Mt.incoh.n_ctrl, Mt.incoh.degree, E);
-    idx[6 * i + 5] = lower_index(D + Mt.rita.energy, 0, Mt.rita.n_energy, E) - 1;
+    // the indices the transport kernel uses (bucketed searches, FP64)
+    long long r[6] = {lin_index_bk<double>(T, T.majorant, E), lin_index_bk<double>(T, Mt.total, E),
+                      lin_index_bk<double>(T, Mt.sfunc, E), spline_span_bk<double>(T, Mt.coh, E),
+                      spline_span_bk<double>(T, Mt.incoh, E), rita_row_bk<double>(T, Mt.rita, E)};
+    // the FP32 bucketed searches must equal full searches of the FP32 node arrays
+    const float Ef = float(E);
+    const float* F = T.f;
+    const long long f_bk[6] = {lin_index_bk<float>(T, T.majorant, Ef), lin_index_bk<float>(T, Mt.total, Ef),
+                               lin_index_bk<float>(T, Mt.sfunc, Ef), spline_span_bk<float>(T, Mt.coh, Ef),
+                               spline_span_bk<float>(T, Mt.incoh, Ef), rita_row_bk<float>(T, Mt.rita, Ef)};
+    const long long f_full[6] = {lin_index(F + T.majorant.x, T.majorant.n, Ef), lin_index(F + Mt.total.x, Mt.total.n, Ef),
+                                 lin_index(F + Mt.sfunc.x, Mt.sfunc.n, Ef),
+                                 spline_span(F + Mt.coh.knot_e, Mt.coh.n_ctrl, Mt.coh.degree, Ef),
+                                 spline_span(F + Mt.incoh.knot_e, Mt.incoh.n_ctrl, Mt.incoh.degree, Ef),
+                                 lower_index(F + Mt.rita.energy, 0, Mt.rita.n_energy, Ef) - 1};
+    for (int k = 0; k < 6; ++k) idx[6 * i + k] = (f_bk[k] == f_full[k]) ? r[k] : -1000;
 }
 
 __global__ void remap_kernel(const uint8_t* in, uint8_t* out, const uint8_t* lut, size_t n, int* bad) {
@@ -362,6 +371,7 @@ struct midsx_gpu_tables {
     double* d = nullptr;
     float* f = nullptr;
     int* rows = nullptr;
+    int* bk = nullptr;
     int32_t ids[MIDSX_MAX_MATERIALS];
     int device = 0;
     int sm_count = 0;
@@ -446,6 +456,72 @@ void fill_spline(DevSpline& o, const midsx_spline_table& t) {
 
 constexpr int kScalarWords = MIDSX_SCALAR_SLOTS;
 
+// Bucket tables of the searched node arrays (lookup.h).  Energies: binade slices of 1/128
+// octave from 128 eV to 256 keV; momentum transfer: 1/64 octave from 2^-8 to 2^5 1/A.
+// Queries outside a window fall in its first or last slice, which still gives the exact
+// index (over a longer search range).
+constexpr int kBucketBits[2] = {7, 6};
+constexpr double kBucketLo[2] = {128.0, 1.0 / 256.0};
+constexpr int kBucketOctaves[2] = {11, 13};
+
+double slice_lo_d(long long key, int kbits) {
+    unsigned long long bits = (unsigned long long)key << (52 - kbits);
+    double v;
+    std::memcpy(&v, &bits, 8);
+    return v;
+}
+float slice_lo_f(long long key, int kbits) {
+    unsigned int bits = (unsigned int)((unsigned long long)key << (23 - kbits));
+    float v;
+    std::memcpy(&v, &bits, 4);
+    return v;
+}
+
+struct BucketBuilder {
+    std::vector<int> data;
+    BucketSpec spec[2][2];
+    BucketBuilder() {
+        for (int k = 0; k < 2; ++k) {
+            int nb = kBucketOctaves[k] << kBucketBits[k];
+            spec[k][0] = {kBucketBits[k], bucket_key(kBucketLo[k], kBucketBits[k]), nb};
+            spec[k][1] = {kBucketBits[k], bucket_key(float(kBucketLo[k]), kBucketBits[k]), nb};
+        }
+    }
+    // mode 0: upper_bound over [lo, hi) (lo = 0, hi = n for LogLogLinear; the knot range for
+    // a spline span); mode 1: lower_bound over [0, n) (RITA energies).
+    template <typename R>
+    int add(const double* x64, int n, int kind, int mode, int lo, int hi) {
+        const BucketSpec& s = spec[kind][sizeof(R) == 8 ? 0 : 1];
+        std::vector<R> x;
+        x.resize(size_t(n));
+        for (int i = 0; i < n; ++i) x[size_t(i)] = R(x64[i]);
+        int off = int(data.size());
+        data.push_back(lo);
+        for (int b = 1; b < s.nb; ++b) {
+            R q = (sizeof(R) == 8) ? R(slice_lo_d(s.base + b, s.kbits)) : R(slice_lo_f(s.base + b, s.kbits));
+            int r = mode == 0 ? int(std::upper_bound(x.begin(), x.end(), q) - x.begin())
+                              : int(std::lower_bound(x.begin(), x.end(), q) - x.begin());
+            data.push_back(std::min(std::max(r, lo), hi));
+        }
+        data.push_back(hi);
+        return off;
+    }
+    void lin(const double* D, DevLin& L, int kind) {
+        L.kind = kind;
+        L.bk_d = add<double>(D + L.x, L.n, kind, 0, 0, L.n);
+        L.bk_f = add<float>(D + L.x, L.n, kind, 0, 0, L.n);
+    }
+    void spline(const double* D, DevSpline& S) {
+        int nk = S.n_ctrl + S.degree + 1;
+        S.bk_d = add<double>(D + S.knot_e, nk, 0, 0, S.degree - 1, nk - S.degree - 1);
+        S.bk_f = add<float>(D + S.knot_e, nk, 0, 0, S.degree - 1, nk - S.degree - 1);
+    }
+    void rita(const double* D, DevRita& Rt) {
+        Rt.bk_d = add<double>(D + Rt.energy, Rt.n_energy, 0, 1, 0, Rt.n_energy);
+        Rt.bk_f = add<float>(D + Rt.energy, Rt.n_energy, 0, 1, 0, Rt.n_energy);
+    }
+};
+
 }  // namespace
 
 extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, midsx_tables_h* out) {
@@ -500,6 +576,26 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
         d.rita.n_energy = s.rita.n_energy;
         h->ids[m] = s.id;
     }
+    // bucket tables for every searched node array, FP64 and FP32 queries
+    BucketBuilder bb;
+    const double* D = blob->data;
+    bb.lin(D, T.majorant, 0);
+    for (int m = 0; m < blob->n_materials; ++m) {
+        DevMaterial& d = T.mat[m];
+        bb.lin(D, d.total, 0);
+        bb.lin(D, d.sfunc, 1);
+        bb.spline(D, d.coh);
+        bb.spline(D, d.incoh);
+        bb.rita(D, d.rita);
+    }
+    for (int k = 0; k < 2; ++k)
+        for (int p = 0; p < 2; ++p) T.bs[k][p] = bb.spec[k][p];
+    if (!cuda_ok(cudaMalloc(&h->bk, bb.data.size() * sizeof(int)), "cudaMalloc")) {
+        midsx_gpu_tables_destroy(h);
+        return MIDSX_OOM;
+    }
+    CUDA_TRY(cudaMemcpy(h->bk, bb.data.data(), bb.data.size() * sizeof(int), cudaMemcpyHostToDevice));
+    T.bk = h->bk;
     *out = h;
     return MIDSX_OK;
 }
@@ -509,6 +605,7 @@ extern "C" midsx_status midsx_gpu_tables_destroy(midsx_tables_h t) {
     cudaFree(t->d);
     cudaFree(t->f);
     cudaFree(t->rows);
+    cudaFree(t->bk);
     delete t;
     return MIDSX_OK;
 }
