@@ -243,8 +243,11 @@ typedef struct midsx_run_config {
     int32_t max_compton_trials;  /* Kahn/S(x) rejection cap (0 = 100000) */
     int32_t block_size;          /* 0 = tuned default */
     int32_t blocks_per_sm;       /* 0 = tuned default */
-    int32_t regroup;             /* lanes of a warp parked on a real collision before the warp runs
-                                    its collisions together (1 = at once; 0 = tuned default) */
+    int32_t regroup;             /* lanes of a warp parked on an event (real collision, history
+                                    start) before the warp runs its events together (1 = at once;
+                                    0 = tuned default) */
+    int32_t chunk;               /* history ids a lane reserves per fetch (0 = 1) */
+    int32_t reserved;
     uint64_t seed;
     uint64_t first_history;      /* history ids [first, first + n) select Philox streams */
     uint64_t n_histories;
@@ -292,6 +295,47 @@ midsx_status midsx_gpu_run_host(midsx_tables_h tables, const midsx_geometry_spec
                                 const midsx_tally_spec* specs, int32_t n_specs, int32_t dose_mode,
                                 const midsx_run_config* cfg, double* dose_sum_out,
                                 midsx_run_stats* stats_out);
+
+/* Non-blocking CUDA stream helpers for C callers without the CUDA runtime headers. */
+midsx_status midsx_gpu_stream_create(void** stream_out);
+midsx_status midsx_gpu_stream_destroy(void* stream);
+midsx_status midsx_gpu_stream_synchronize(void* stream);  /* with the MIDSX_WAIT_TIMEOUT_S deadline */
+
+/* ---------------------------------------------------------------- batched launches --- */
+/* Several independent simulations (different phantoms, sources, tallies, history counts and
+ * seeds; one shared set of tables) transported by one persistent launch: history indices
+ * over the concatenation of the jobs are handed out dynamically to the lanes, so jobs of
+ * very different sizes finish together.  No reference counterpart (MIDSX runs one simulation
+ * per runSimulation call); each job's results equal those of a single run of that job with
+ * the same seed and history range (same Philox streams, integer tallies in the mixed form). */
+#define MIDSX_MAX_BATCH_JOBS 64
+typedef struct midsx_gpu_batch* midsx_batch_h;
+
+typedef struct midsx_batch_job {
+    midsx_phantom_h phantom;   /* created with the batch's tables */
+    midsx_source_h source;
+    midsx_tallies_h tallies;
+    uint64_t seed;
+    uint64_t first_history;    /* histories [first + e * n, first + (e + 1) * n) in epoch e */
+    uint64_t n_histories;
+} midsx_batch_job;
+
+midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const midsx_batch_job* jobs, int32_t n_jobs,
+                                    midsx_batch_h* out);
+midsx_status midsx_gpu_batch_destroy(midsx_batch_h b);
+/* One launch over every job (cfg: precision and launch shape; its seed/first/n are unused),
+ * then the batch's epoch advances so that the next run transports the next histories. */
+midsx_status midsx_gpu_batch_run(midsx_batch_h b, const midsx_run_config* cfg, void* stream);
+/* Captures one run (counter reset, persistent launch, epoch advance) into a CUDA graph on
+ * `stream`; midsx_gpu_batch_replay launches it.  Replays advance the epoch like runs. */
+midsx_status midsx_gpu_batch_capture(midsx_batch_h b, const midsx_run_config* cfg, void* stream);
+midsx_status midsx_gpu_batch_replay(midsx_batch_h b, void* stream);
+/* Times candidate launch shapes (block size, blocks per SM, regroup threshold, histories
+ * per fetch) on `trial_histories` histories spread over the jobs in proportion to their
+ * sizes, returns the fastest in *best (precision as given) and its histories/s; the trial
+ * runs leave the jobs' tallies reset and the epoch unchanged.  Synchronous. */
+midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precision, uint64_t trial_histories,
+                                      midsx_run_config* best, double* best_rate, void* stream);
 
 /* ----------------------------------------------------------- sampler diagnostics --- */
 /* Draw n samples of one sampler on the device with the transport kernel's own device

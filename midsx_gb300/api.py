@@ -292,9 +292,11 @@ class Tallies:
 PRECISIONS = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}
 
 
-def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0, regroup=0):
+def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0, regroup=0,
+               chunk=0):
     c = N.RunConfig()
     c.regroup = int(regroup)
+    c.chunk = int(chunk)
     c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     c.n_histories = int(n)
     c.seed = int(seed)
@@ -311,6 +313,80 @@ def run(tables, phantom, source, tallies, n, seed, first=0, precision="mixed", s
     cfg = run_config(n, seed, first, precision, **kw)
     N.check(N.load().midsx_gpu_run(tables.handle, phantom.handle, source.handle, tallies.handle, C.byref(cfg),
                                    stream), "midsx_gpu_run")
+
+
+class Stream:
+    """A non-blocking CUDA stream (midsx_gpu_stream_*); .handle is the cudaStream_t."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        N.check(N.load().midsx_gpu_stream_create(C.byref(h)), "midsx_gpu_stream_create")
+        self.handle = h
+
+    def synchronize(self):
+        N.check(N.load().midsx_gpu_stream_synchronize(self.handle), "midsx_gpu_stream_synchronize")
+
+    def close(self):
+        if self.handle:
+            N.load().midsx_gpu_stream_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Several simulations transported by one persistent launch (midsx_gpu_batch_*).
+    jobs: list of (phantom, source, tallies, seed, first, n)."""
+
+    def __init__(self, tables, jobs):
+        self.tables = tables
+        self.jobs = list(jobs)
+        arr = (N.BatchJob * len(self.jobs))()
+        for i, (ph, src, tl, seed, first, n) in enumerate(self.jobs):
+            arr[i].phantom, arr[i].source, arr[i].tallies = ph.handle, src.handle, tl.handle
+            arr[i].seed, arr[i].first_history, arr[i].n_histories = int(seed), int(first), int(n)
+        h = C.c_void_p()
+        N.check(N.load().midsx_gpu_batch_create(tables.handle, arr, len(self.jobs), C.byref(h)),
+                "midsx_gpu_batch_create")
+        self.handle = h
+
+    @property
+    def histories(self):
+        return sum(int(j[5]) for j in self.jobs)
+
+    def run(self, precision="mixed", stream=None, **launch):
+        cfg = run_config(0, 0, 0, precision, **launch)
+        N.check(N.load().midsx_gpu_batch_run(self.handle, C.byref(cfg), stream), "midsx_gpu_batch_run")
+
+    def capture(self, stream, precision="mixed", **launch):
+        cfg = run_config(0, 0, 0, precision, **launch)
+        N.check(N.load().midsx_gpu_batch_capture(self.handle, C.byref(cfg), stream), "midsx_gpu_batch_capture")
+
+    def replay(self, stream):
+        N.check(N.load().midsx_gpu_batch_replay(self.handle, stream), "midsx_gpu_batch_replay")
+
+    def autotune(self, precision="mixed", trial=2_000_000, stream=None):
+        best = N.RunConfig()
+        rate = C.c_double()
+        N.check(N.load().midsx_gpu_batch_autotune(self.handle, PRECISIONS[precision], int(trial), C.byref(best),
+                                                  C.byref(rate), stream), "midsx_gpu_batch_autotune")
+        launch = dict(block=best.block_size, per_sm=best.blocks_per_sm, regroup=best.regroup, chunk=best.chunk)
+        return launch, rate.value
+
+    def close(self):
+        if self.handle:
+            N.load().midsx_gpu_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def trace_deposits(tables, phantom, source, n, seed, first=0, precision="fp64", **kw):

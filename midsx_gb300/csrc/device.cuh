@@ -218,6 +218,7 @@ struct DevSpline {
     int knot_e, knot_u, ctrl, n_ctrl, degree;
     int bk_d, bk_f;
     double lx_min, lx_max;
+    float f_lx_min, f_lx_max;  // FP32 copies for the mixed form
 };
 struct DevRita {
     int energy, log_energy, row_start, x, y, a, b, n_energy;
@@ -236,6 +237,7 @@ struct DevTables {
     BucketSpec bs[2][2];  // [kind][0 = FP64 query, 1 = FP32 query]
     int n_materials;
     double alpha;        // 1/Angstrom per unit k
+    float alpha_f;       // FP32 copy
     double e_max;
     DevLin majorant;
     DevMaterial mat[MIDSX_MAX_MATERIALS];
@@ -292,7 +294,15 @@ template <typename R>
 MIDSX_HD R spline_lookup(const DevTables& t, const DevSpline& S, R e) {
     const R* D = tab<R>(t);
     int span = spline_span_bk<R>(t, S, e);
-    return spline_eval_at(D + S.knot_u, D + S.ctrl, S.degree, span, R(S.lx_min), R(S.lx_max), e);
+    R lo, hi;
+    if constexpr (sizeof(R) == 8) {
+        lo = S.lx_min;
+        hi = S.lx_max;
+    } else {
+        lo = S.f_lx_min;
+        hi = S.f_lx_max;
+    }
+    return spline_eval_at(D + S.knot_u, D + S.ctrl, S.degree, span, lo, hi, e);
 }
 
 // Lower RITA energy row (lower_bound - 1) with the bucketed search.
@@ -333,7 +343,19 @@ struct DevTally {
     double norm[3];      // plane normal used for the entrance cosine
     double e1e1, e2e2;   // rectangle basis dot products
     unsigned long long* acc;
+    // FP32 copies for the mixed form
+    float fa[3], fb[3], fc[3], fnorm[3];
+    float fradius, fe1e1, fe2e2;
 };
+
+// The working-precision value of a field stored in FP64 with an FP32 copy.
+template <typename R>
+MIDSX_HD R pickr(double d, float f) {
+    if constexpr (sizeof(R) == 8)
+        return d;
+    else
+        return f;
+}
 
 // fixed-point scales of the mixed path (per eV, per eV^2, per unit cosine)
 constexpr double kFxEnergy = 4096.0;

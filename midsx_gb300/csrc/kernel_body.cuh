@@ -1,16 +1,22 @@
 // kernel_body.cuh - the transport kernel (included by transport.cu).
 //
-// Layout of the work: every lane of a warp owns one history at a time (history ids strided by
-// the number of threads).  Each loop iteration is one Woodcock step
-// (src/MIDSX/Core/physics_engine.cpp:28-79) for every lane that is flying.  The long, rare
-// pieces of work are "events": a real collision (interaction type, Rayleigh / Compton /
-// photoelectric sampling, tallies, dose) and the start of a new history (source sampling and
-// the per-energy table lookups).  A lane that needs an event parks; the warp runs the parked
-// events once `regroup` of its lanes wait - or no lane is left flying - so that event code
-// runs with many lanes active instead of one (warp ballot; each interaction type is then a
-// branch of its own).  Per-history counters stay in 32-bit registers and are flushed to
-// shared-memory block counters when the history ends; one atomic per block and counter at
-// the end.
+// Layout of the work: every lane of a warp owns one history at a time.  Each loop iteration
+// is one Woodcock step (src/MIDSX/Core/physics_engine.cpp:28-79) for every lane that is
+// flying.  The long, rare pieces of work are "events": a real collision (interaction type,
+// Rayleigh / Compton / photoelectric sampling, tallies, dose) and the start of a new history
+// (history id, source sampling, per-energy table lookups).  A lane that needs an event
+// parks; the warp runs the parked events once `regroup` of its lanes wait - or no lane is
+// left flying - so that event code runs with many lanes active instead of one (warp ballot;
+// each interaction type is then a branch of its own).
+//
+// Work distribution: history indices are handed out by one atomic per warp start-event
+// (`chunk` indices per starting lane), so fast and slow histories balance across the whole
+// grid.  A single-job launch takes its job from the kernel parameters; a batched launch
+// (MULTI) maps each index to a job through the launch's prefix table and reads the job's
+// geometry from shared memory, so simulations with different phantoms, sources and history
+// counts run together in one persistent launch.  Per-history counters stay in 32-bit
+// registers and are flushed to shared-memory per-job counters when the history ends; one
+// atomic per block, job and counter at the end.
 
 // per-energy cache: majorant and every material's total cross section and delta-scatter
 // threshold (isDeltaScatter: p_delta = 1 - mu / mu_max), kept per thread in shared memory
@@ -30,7 +36,11 @@ __device__ __noinline__ R refresh_energy(const RunParams& P, R E, R* thr, R* mu,
 template <typename R>
 __device__ __noinline__ bool sample_compton(const RunParams& P, const DevMaterial& Mt, HistoryRng& rng, R E, R& mu,
                                             R& kp, uint32_t& trials) {
-    const R alpha = R(P.T.alpha);
+    R alpha;
+    if constexpr (sizeof(R) == 8)
+        alpha = P.T.alpha;
+    else
+        alpha = P.T.alpha_f;
     const R k = E / R(kMec2);
     const R r1p = (R(1) + R(2) * k) / (R(9) + R(2) * k);
     const R s_max = lin_lookup<R>(P.T, Mt.sfunc, alpha * k * sqrt_(R(2)));
@@ -55,11 +65,11 @@ __device__ __noinline__ bool sample_compton(const RunParams& P, const DevMateria
     return false;
 }
 
-template <bool MX>
-__device__ __noinline__ void score_dose(const RunParams& P, int vox, double dep) {
-    unsigned long long* rec = P.dose + size_t(vox) * P.dose_stride;
+template <typename R, bool MX>
+__device__ __noinline__ void score_dose(unsigned long long* dose, int stride, int vox, R dep) {
+    unsigned long long* rec = dose + size_t(vox) * stride;
     Acc<MX>::energy(rec, dep);
-    if (P.dose_stride > 1) {
+    if (stride > 1) {
         Acc<MX>::energy2(rec + 1, dep);
         count1(rec + 2);
     }
@@ -69,62 +79,105 @@ __device__ __forceinline__ void stat_add(unsigned long long* s, int slot, unsign
     if (v) atomicAdd(s + slot, v);
 }
 
+// statistics energies in fixed point (1/1024 eV); the FP32 form converts with a 32-bit
+// conversion (energies below 4 MeV)
 __device__ __forceinline__ unsigned long long fx_stat(double e) { return (unsigned long long)llrint(e * kFxStat); }
+__device__ __forceinline__ unsigned long long fx_stat(float e) {
+    return (unsigned long long)__float2uint_rn(e * float(kFxStat));
+}
+
+// Geometry of one job in the working precision (ComputationalDomain with one voxel grid).
+template <typename R>
+struct Geo {
+    V3<R> dom, org, ext, spc, ispc;
+    int nx, ny, nz, bg;
+    const uint8_t* ids;
+};
 
 template <typename R>
+__device__ Geo<R> make_geo(const DevGeom& G) {
+    Geo<R> g;
+    g.dom = {R(G.domain[0]), R(G.domain[1]), R(G.domain[2])};
+    g.org = {R(G.origin[0]), R(G.origin[1]), R(G.origin[2])};
+    g.ext = {R(G.ext[0]), R(G.ext[1]), R(G.ext[2])};
+    g.spc = {R(G.spacing[0]), R(G.spacing[1]), R(G.spacing[2])};
+    g.ispc = {R(1) / g.spc.x, R(1) / g.spc.y, R(1) / g.spc.z};
+    g.nx = G.dims[0];
+    g.ny = G.dims[1];
+    g.nz = G.dims[2];
+    g.bg = G.background;
+    g.ids = G.ids;
+    return g;
+}
+
+// Shared-memory bytes of a launch: per-job counters, the batch's prefix table and geometry,
+// then the per-thread energy cache.
+template <typename R>
+__host__ __device__ inline size_t kernel_smem(int n_jobs, bool multi, int n_materials, int block) {
+    size_t b = size_t(n_jobs) * kStCount * 8;
+    if (multi) b += size_t(n_jobs + 1) * 8 + size_t(n_jobs) * sizeof(Geo<R>);
+    b = (b + 15) & ~size_t(15);
+    return b + size_t(2) * n_materials * block * sizeof(R);
+}
+
+template <typename R, bool MULTI>
 __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
     constexpr bool MX = sizeof(R) == 4;
-    extern __shared__ unsigned char smem_raw[];
-    __shared__ unsigned long long s_stats[kStCount];
-    R* cache = reinterpret_cast<R*>(smem_raw);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int njobs = MULTI ? P.n_jobs : 1;
+    unsigned long long* s_stats = reinterpret_cast<unsigned long long*>(smem_raw);
+    unsigned long long* s_prefix = s_stats + njobs * kStCount;
+    Geo<R>* s_geo = reinterpret_cast<Geo<R>*>(s_prefix + (MULTI ? njobs + 1 : 0));
+    size_t head = size_t(njobs) * kStCount * 8 + (MULTI ? size_t(njobs + 1) * 8 + size_t(njobs) * sizeof(Geo<R>) : 0);
+    R* cache = reinterpret_cast<R*>(smem_raw + ((head + 15) & ~size_t(15)));
     const int stride = blockDim.x;
     const int M = P.T.n_materials;
     R* thr = cache + threadIdx.x;
     R* mucache = cache + M * stride + threadIdx.x;
-    if (threadIdx.x < kStCount) s_stats[threadIdx.x] = 0;
+    for (int i = threadIdx.x; i < njobs * kStCount; i += blockDim.x) s_stats[i] = 0;
+    if (MULTI) {
+        for (int i = threadIdx.x; i <= njobs; i += blockDim.x) s_prefix[i] = P.prefix[i];
+        for (int i = threadIdx.x; i < njobs; i += blockDim.x) s_geo[i] = make_geo<R>(P.jobs[i].G);
+    }
     __syncthreads();
+    const Geo<R> g0 = make_geo<R>(P.job0.G);  // single-job launches
+    const unsigned long long epoch = P.epoch ? *P.epoch : 0ull;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lanes_below = (1u << lane) - 1u;
 
-    const V3<R> dom = {R(P.G.domain[0]), R(P.G.domain[1]), R(P.G.domain[2])};
-    const V3<R> org = {R(P.G.origin[0]), R(P.G.origin[1]), R(P.G.origin[2])};
-    const V3<R> ext = {R(P.G.ext[0]), R(P.G.ext[1]), R(P.G.ext[2])};
-    const V3<R> spc = {R(P.G.spacing[0]), R(P.G.spacing[1]), R(P.G.spacing[2])};
-    // the FP32 form multiplies by reciprocals (voxel index, free path); the FP64 form divides
-    // exactly as the reference does
-    const V3<R> ispc = {R(1) / spc.x, R(1) / spc.y, R(1) / spc.z};
-    const int nx = P.G.dims[0], ny = P.G.dims[1], nz = P.G.dims[2];
-    const bool have_tallies = P.n_tallies > 0;
-    const uint64_t total_threads = uint64_t(gridDim.x) * blockDim.x;
-
-    uint64_t h = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;  // current / next history id
-    bool alive = false, pending = false;
+    bool alive = false, pending = false, exhausted = false;
+    unsigned long long next = 0, end = 0, gidx = 0;
+    int job = 0, ntal = 0;
     HistoryRng rng;
     V3<R> pos, dir, p0;
     R E = R(0), mu_max = R(0), inv_mu_max = R(0), s = R(0);
     int n_coh = 0, n_incoh = 0, vox = -1, mat = 0;
     uint32_t steps = 0, fetches = 0, trials = 0, words = 0;
-    double hist_dep = 0.0;
+    R hist_dep = R(0);
     unsigned mask = 0xffffffffu;
 
     auto end_history = [&]() {
-        if (P.trace) P.trace[h] = hist_dep;
-        stat_add(s_stats, kStSteps, steps);
-        stat_add(s_stats, kStFetches, fetches);
-        stat_add(s_stats, kStTrials, trials);
-        stat_add(s_stats, kStWords, words);
+        if (!MULTI && P.trace) P.trace[gidx] = hist_dep;
+        unsigned long long* st = s_stats + job * kStCount;
+        stat_add(st, kStSteps, steps);
+        stat_add(st, kStFetches, fetches);
+        stat_add(st, kStTrials, trials);
+        stat_add(st, kStWords, words);
         alive = false;
         pending = false;
-        h += total_threads;
     };
 
     for (;;) {
-        const bool done = !alive && h >= P.n;
+        const bool done = !alive && exhausted;
         mask = __ballot_sync(mask, !done);
         if (done) break;
+        const Geo<R>& g = MULTI ? s_geo[job] : g0;
+        unsigned long long* st = s_stats + job * kStCount;
         bool finish = false;  // the history ends in this iteration
         if (alive && !pending) {
             // one Woodcock step: getFreePath, move, domain test, voxel fetch, isDeltaScatter
             if (steps >= uint32_t(P.max_steps)) {
-                stat_add(s_stats, kStStepCap, 1);
+                stat_add(st, kStStepCap, 1);
                 finish = true;
             } else {
                 ++steps;
@@ -136,41 +189,49 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                     s = -log_(to_uniform(w1, R(0))) / mu_max;
                 p0 = pos;
                 pos = {pos.x + s * dir.x, pos.y + s * dir.y, pos.z + s * dir.z};
-                if (!(pos.x >= R(0) && pos.x <= dom.x && pos.y >= R(0) && pos.y <= dom.y && pos.z >= R(0) &&
-                      pos.z <= dom.z)) {
-                    if (have_tallies)
-                        score_tallies<R, MX>(P, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false, R(0), words);
-                    stat_add(s_stats, kStEscE, fx_stat(double(E)));
+                if (!(pos.x >= R(0) && pos.x <= g.dom.x && pos.y >= R(0) && pos.y <= g.dom.y && pos.z >= R(0) &&
+                      pos.z <= g.dom.z)) {
+                    if (ntal) {
+                        const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
+                        score_tallies<R, MX>(tal, ntal, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false, R(0),
+                                             words);
+                    }
+                    stat_add(st, kStEscE, fx_stat(E));
                     finish = true;
                 } else {
-                    const V3<R> q = {pos.x - org.x, pos.y - org.y, pos.z - org.z};
+                    const V3<R> q = {pos.x - g.org.x, pos.y - g.org.y, pos.z - g.org.z};
                     vox = -1;
-                    mat = P.G.background;
-                    if (q.x >= R(0) && q.x <= ext.x && q.y >= R(0) && q.y <= ext.y && q.z >= R(0) && q.z <= ext.z) {
+                    mat = g.bg;
+                    if (q.x >= R(0) && q.x <= g.ext.x && q.y >= R(0) && q.y <= g.ext.y && q.z >= R(0) &&
+                        q.z <= g.ext.z) {
                         int ix, iy, iz;
                         if constexpr (MX) {
-                            ix = int(q.x * ispc.x);
-                            iy = int(q.y * ispc.y);
-                            iz = int(q.z * ispc.z);
+                            // the FP32 form multiplies by the reciprocal voxel size; the FP64
+                            // form divides exactly as the reference does
+                            ix = int(q.x * g.ispc.x);
+                            iy = int(q.y * g.ispc.y);
+                            iz = int(q.z * g.ispc.z);
                         } else {
-                            ix = int(q.x / spc.x);
-                            iy = int(q.y / spc.y);
-                            iz = int(q.z / spc.z);
+                            ix = int(q.x / g.spc.x);
+                            iy = int(q.y / g.spc.y);
+                            iz = int(q.z / g.spc.z);
                         }
-                        if (ix >= nx || iy >= ny || iz >= nz) {
-                            stat_add(s_stats, kStEdge, 1);  // the reference's vector::at would throw here
-                            ix = min(ix, nx - 1);
-                            iy = min(iy, ny - 1);
-                            iz = min(iz, nz - 1);
+                        if (ix >= g.nx || iy >= g.ny || iz >= g.nz) {
+                            stat_add(st, kStEdge, 1);  // the reference's vector::at would throw here
+                            ix = min(ix, g.nx - 1);
+                            iy = min(iy, g.ny - 1);
+                            iz = min(iz, g.nz - 1);
                         }
-                        vox = ix + iy * nx + iz * nx * ny;
-                        mat = __ldg(P.G.ids + vox);
+                        vox = ix + iy * g.nx + iz * g.nx * g.ny;
+                        mat = __ldg(g.ids + vox);
                         ++fetches;
                     }
                     if (to_uniform(w2, R(0)) < thr[mat * stride]) {
-                        if (have_tallies)
-                            score_tallies<R, MX>(P, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false, R(0),
-                                                 words);
+                        if (ntal) {
+                            const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
+                            score_tallies<R, MX>(tal, ntal, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false,
+                                                 R(0), words);
+                        }
                     } else {
                         pending = true;  // a real collision: an event
                     }
@@ -179,23 +240,61 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
         }
         if (finish) end_history();
         // events: run the parked collisions and history starts once enough lanes wait
-        const bool want = pending || (!alive && h < P.n);
+        const bool want = pending || (!alive && !exhausted);
         const unsigned wmask = __ballot_sync(mask, want);
         const unsigned fmask = __ballot_sync(mask, alive && !pending);
-        if (want && (__popc(wmask) >= P.regroup || fmask == 0u)) {
+        const bool go = __popc(wmask) >= P.regroup || fmask == 0u;
+        const unsigned start_mask = go ? (wmask & ~__ballot_sync(mask, alive)) : 0u;
+        if (want && go) {
             finish = false;
             if (!alive) {
-                // PhotonSource::generatePhoton + a fresh per-history stream
-                rng.init(P.seed, P.first + h);
-                sample_source<R>(P.S, rng, pos, dir, E);
-                stat_add(s_stats, kStHistories, 1);
-                stat_add(s_stats, kStSourceE, fx_stat(double(E)));
-                n_coh = n_incoh = 0;
-                steps = fetches = trials = words = 0;
-                hist_dep = 0.0;
-                mu_max = refresh_energy<R>(P, E, thr, mucache, stride);
-                inv_mu_max = R(1) / mu_max;
-                alive = true;
+                // hand out history indices: one atomic per warp for the lanes that hold none
+                const unsigned need = __ballot_sync(start_mask, next >= end);
+                if (next >= end) {
+                    const int leader = __ffs(need) - 1;
+                    unsigned long long base = 0;
+                    if (int(lane) == leader)
+                        base = atomicAdd(P.counter, (unsigned long long)__popc(need) * (unsigned long long)P.chunk);
+                    base = __shfl_sync(need, base, leader);
+                    next = base + (unsigned long long)__popc(need & lanes_below) * P.chunk;
+                    end = next + P.chunk;
+                    if (end > P.total) end = P.total;
+                }
+                if (next >= P.total) {
+                    exhausted = true;
+                } else {
+                    gidx = next++;
+                    uint64_t seed, hid;
+                    if (MULTI) {
+                        int lo = 0, hi = njobs;  // last job with prefix <= gidx
+                        while (hi - lo > 1) {
+                            int mid = (lo + hi) >> 1;
+                            if (s_prefix[mid] <= gidx) lo = mid;
+                            else hi = mid;
+                        }
+                        job = lo;
+                        const DevJob& J = P.jobs[job];
+                        seed = J.seed;
+                        hid = J.first + epoch * J.n + (gidx - s_prefix[job]);
+                        ntal = J.n_tallies;
+                    } else {
+                        seed = P.job0.seed;
+                        hid = P.job0.first + epoch * P.job0.n + gidx;
+                        ntal = P.job0.n_tallies;
+                    }
+                    // PhotonSource::generatePhoton + a fresh per-history stream
+                    rng.init(seed, hid);
+                    sample_source<R>(MULTI ? P.jobs[job].S : P.job0.S, rng, pos, dir, E);
+                    unsigned long long* sj = s_stats + job * kStCount;
+                    stat_add(sj, kStHistories, 1);
+                    stat_add(sj, kStSourceE, fx_stat(E));
+                    n_coh = n_incoh = 0;
+                    steps = fetches = trials = words = 0;
+                    hist_dep = R(0);
+                    mu_max = refresh_energy<R>(P, E, thr, mucache, stride);
+                    inv_mu_max = R(1) / mu_max;
+                    alive = true;
+                }
             } else {
                 pending = false;
                 // setInteractionType (physics_engine.cpp:82-109)
@@ -212,10 +311,10 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                 if (u3 < p_coh) {
                     // CoherentScattering::interact
                     ++n_coh;
-                    stat_add(s_stats, kStCoh, 1);
+                    stat_add(st, kStCoh, 1);
                     R mu;
                     if (!rita_sample<R>(P.T, Mt.rita, E, uniform<R>(rng), mu)) {
-                        stat_add(s_stats, kStRangeErr, 1);
+                        stat_add(st, kStRangeErr, 1);
                         failed = true;
                     } else {
                         R theta = acos_(mu);
@@ -225,10 +324,10 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                 } else if (u3 < p_coh + p_incoh) {
                     // IncoherentScattering::interact
                     ++n_incoh;
-                    stat_add(s_stats, kStIncoh, 1);
+                    stat_add(st, kStIncoh, 1);
                     R mu = R(1), kp = E / R(kMec2);
                     if (!sample_compton<R>(P, Mt, rng, E, mu, kp, trials)) {
-                        stat_add(s_stats, kStTrialCap, 1);
+                        stat_add(st, kStTrialCap, 1);
                         failed = true;
                     } else {
                         const R k = E / R(kMec2);
@@ -241,33 +340,37 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                     }
                 } else {
                     // PhotoelectricEffect::interact
-                    stat_add(s_stats, kStPhoto, 1);
+                    stat_add(st, kStPhoto, 1);
                     dep = E;
                     finish = true;
                 }
                 if (failed) {
                     finish = true;
                 } else {
-                    if (have_tallies)
-                        score_tallies<R, MX>(P, p0, d0, s, E0, cls0, scatter_class(n_coh, n_incoh), true, dep, words);
+                    if (ntal) {
+                        const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
+                        score_tallies<R, MX>(tal, ntal, p0, d0, s, E0, cls0, scatter_class(n_coh, n_incoh), true, dep,
+                                             words);
+                    }
                     if (dep != R(0)) {
                         if (vox >= 0) {
-                            stat_add(s_stats, kStDepGrid, fx_stat(double(dep)));
-                            hist_dep += double(dep);
-                            if (P.dose_stride) {
-                                score_dose<MX>(P, vox, double(dep));
+                            stat_add(st, kStDepGrid, fx_stat(dep));
+                            hist_dep += dep;
+                            const DevJob& J = MULTI ? P.jobs[job] : P.job0;
+                            if (J.dose_stride) {
+                                score_dose<R, MX>(J.dose, J.dose_stride, vox, dep);
                                 ++words;
                             }
                         } else {
-                            stat_add(s_stats, kStDepBg, fx_stat(double(dep)));
+                            stat_add(st, kStDepBg, fx_stat(dep));
                         }
                     }
                     if (!finish) {
                         if (!(fabs_(dir.x) <= R(2) && fabs_(dir.y) <= R(2) && fabs_(dir.z) <= R(2))) {
                             // a NaN direction (RITA rows below ~400 eV are NaN, as in the
                             // reference); its next step would leave the domain: retire the history
-                            stat_add(s_stats, kStNonFinite, 1);
-                            stat_add(s_stats, kStEscE, fx_stat(double(E)));
+                            stat_add(st, kStNonFinite, 1);
+                            stat_add(st, kStEscE, fx_stat(E));
                             finish = true;
                         } else if (energy_changed) {
                             mu_max = refresh_energy<R>(P, E, thr, mucache, stride);
@@ -275,10 +378,20 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                         }
                     }
                 }
+                if (finish) end_history();
             }
-            if (finish) end_history();
         }
     }
     __syncthreads();
-    if (threadIdx.x < kStCount && s_stats[threadIdx.x]) atomicAdd(P.stats + threadIdx.x, s_stats[threadIdx.x]);
+    for (int i = threadIdx.x; i < njobs * kStCount; i += blockDim.x) {
+        const unsigned long long v = s_stats[i];
+        if (v) {
+            const int j = i / kStCount;
+            unsigned long long* dst = MULTI ? P.jobs[j].stats : P.job0.stats;
+            atomicAdd(dst + (i - j * kStCount), v);
+        }
+    }
 }
+
+// Graph replays of a batch advance its epoch so that each replay transports fresh histories.
+__global__ void advance_epoch_kernel(unsigned long long* epoch) { *epoch += 1ull; }

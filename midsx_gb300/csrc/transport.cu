@@ -48,6 +48,11 @@ struct DevSource {
     int n_bins;
     const double* energy;
     const double* cdf;
+    // FP32 copies for the mixed form
+    float f_pos[3], f_a[3], f_b[3], f_c[3];
+    float f_radius, f_mono;
+    const float* f_energy;
+    const float* f_cdf;
 };
 
 struct DevGeom {
@@ -57,19 +62,34 @@ struct DevGeom {
     const uint8_t* ids;
 };
 
-struct RunParams {
-    DevTables T;
+// One simulation: geometry, source, tallies and its history range [first, first + n) of its
+// own Philox key.  A launch runs one job (by value in RunParams) or a batch (device array).
+struct DevJob {
     DevGeom G;
     DevSource S;
     const DevTally* tallies;
     int n_tallies;
     int dose_stride;  // 0 = no dose tally, 1 = sum, 4 = count/sum/sumsq record
     unsigned long long* dose;
-    unsigned long long* stats;
+    unsigned long long* stats;  // kStCount counters of this job
     uint64_t seed, first, n;
+};
+
+constexpr int kMaxBatchJobs = 64;  // jobs of one batched launch (geometry staged in shared memory)
+
+struct RunParams {
+    DevTables T;
+    DevJob job0;                            // single-job launch
+    const DevJob* jobs;                     // batched launch: n_jobs descriptors (device)
+    int n_jobs;
+    const unsigned long long* prefix;       // batched launch: n_jobs + 1 history offsets (device)
+    unsigned long long* counter;            // histories handed out so far (zeroed before launch)
+    unsigned long long total;               // histories of this launch
+    const unsigned long long* epoch;        // optional: history ids advance by n per epoch
     int max_steps, max_trials;
-    int regroup;    // lanes of a warp that wait for a real collision before the warp runs them
-    double* trace;  // optional: energy deposited in grid voxels per history
+    int regroup;    // lanes of a warp that wait for an event before the warp runs the events
+    int chunk;      // histories a lane reserves per fetch
+    double* trace;  // optional (single job): energy deposited in grid voxels per history
 };
 
 // -------------------------------------------------------------------- atomics ---
@@ -88,19 +108,23 @@ struct Acc<false> {  // FP64 plain form
     }
 };
 
+// 64-bit fixed point, exact and order independent.  Values arrive in FP32 and are scaled by
+// powers of two and converted with 32-bit conversions (no double-precision instruction):
+// energies up to kMixedMaxEnergy eV (energy^2 / 16 stays below 2^32), cosines in [0, 1].
+constexpr double kMixedMaxEnergy = 262144.0;
 template <>
-struct Acc<true> {  // 64-bit fixed point, exact and order independent
-    __device__ static void energy(unsigned long long* p, double v) {
-        atomicAdd(p, (unsigned long long)__double2ll_rn(v * kFxEnergy));
+struct Acc<true> {
+    __device__ static void energy(unsigned long long* p, float v) {
+        atomicAdd(p, (unsigned long long)__float2uint_rn(v * float(kFxEnergy)));
     }
-    __device__ static void energy2(unsigned long long* p, double v) {
-        atomicAdd(p, (unsigned long long)__double2ll_rn(v * v * kFxEnergy2));
+    __device__ static void energy2(unsigned long long* p, float v) {
+        atomicAdd(p, (unsigned long long)__float2uint_rn(v * v * float(kFxEnergy2)));
     }
-    __device__ static void cosine(unsigned long long* p, double v) {
-        atomicAdd(p, (unsigned long long)__double2ll_rn(v * kFxCosine));
+    __device__ static void cosine(unsigned long long* p, float v) {
+        atomicAdd(p, (unsigned long long)__float2uint_rn(v * float(kFxCosine)));
     }
-    __device__ static void cosine2(unsigned long long* p, double v) {
-        atomicAdd(p, (unsigned long long)__double2ll_rn(v * v * kFxCosine));
+    __device__ static void cosine2(unsigned long long* p, float v) {
+        atomicAdd(p, (unsigned long long)__float2uint_rn(v * v * float(kFxCosine)));
     }
 };
 
@@ -109,9 +133,9 @@ __device__ __forceinline__ void count1(unsigned long long* p) { atomicAdd(p, 1ul
 // ------------------------------------------------------------------ tally scoring ---
 // VectorVolumeQuantity / VectorSurfaceQuantity::measure: skip zero values, else add
 // (count, sum, sum of squares) to the class.
-template <bool MX>
-__device__ __forceinline__ void vec_energy(unsigned long long* acc, int q, int cls, double v, uint32_t& words) {
-    if (v == 0.0) return;
+template <typename R, bool MX>
+__device__ __forceinline__ void vec_energy(unsigned long long* acc, int q, int cls, R v, uint32_t& words) {
+    if (v == R(0)) return;
     unsigned long long* s = acc + q * 12 + cls * 3;
     count1(s);
     Acc<MX>::energy(s + 1, v);
@@ -119,9 +143,9 @@ __device__ __forceinline__ void vec_energy(unsigned long long* acc, int q, int c
     ++words;  // one accumulator record (count, sum, sum of squares) updated
 }
 
-template <bool MX>
-__device__ __forceinline__ void vec_cosine(unsigned long long* acc, int q, int cls, double v, uint32_t& words) {
-    if (v == 0.0) return;
+template <typename R, bool MX>
+__device__ __forceinline__ void vec_cosine(unsigned long long* acc, int q, int cls, R v, uint32_t& words) {
+    if (v == R(0)) return;
     unsigned long long* s = acc + q * 12 + cls * 3;
     count1(s);
     Acc<MX>::cosine(s + 1, v);
@@ -134,10 +158,10 @@ __device__ __forceinline__ void vec_cosine(unsigned long long* acc, int q, int c
 // cls1: class of final_photon (post-interaction counts if the step interacted, else
 // a default Photon = primary), used by volume quantities.
 template <typename R, bool MX>
-__device__ __noinline__ void score_tallies(const RunParams& P, const V3<R>& p0, const V3<R>& d, R s, R E, int cls0,
-                              int cls1, bool interact, R dep, uint32_t& words) {
-    for (int ti = 0; ti < P.n_tallies; ++ti) {
-        const DevTally& T = P.tallies[ti];
+__device__ __noinline__ void score_tallies(const DevTally* tallies, int n_tallies, const V3<R>& p0, const V3<R>& d,
+                                           R s, R E, int cls0, int cls1, bool interact, R dep, uint32_t& words) {
+    for (int ti = 0; ti < n_tallies; ++ti) {
+        const DevTally& T = tallies[ti];
         const int kind = T.kind;
         if (kind == MIDSX_TALLY_VOLUME_AACUBOID) {
             // AACuboidVolumeTally::determineVolumeTraversal (volume_tally.cpp:38-91)
@@ -151,8 +175,8 @@ __device__ __noinline__ void score_tallies(const RunParams& P, const V3<R>& p0, 
                     hi[i] = R(INFINITY);
                     continue;
                 }
-                lo[i] = (R(T.a[i]) - pp[i]) / dd[i];
-                hi[i] = (R(T.b[i]) - pp[i]) / dd[i];
+                lo[i] = (pickr<R>(T.a[i], T.fa[i]) - pp[i]) / dd[i];
+                hi[i] = (pickr<R>(T.b[i], T.fb[i]) - pp[i]) / dd[i];
                 if (lo[i] > hi[i]) {
                     R tmp = lo[i];
                     lo[i] = hi[i];
@@ -174,9 +198,9 @@ __device__ __noinline__ void score_tallies(const RunParams& P, const V3<R>& p0, 
                 e_dep = (exit_ < s) ? R(0) : dep;   // PASSES_THROUGH zeroes, LANDS_INSIDE keeps
             }
             unsigned long long* acc = T.acc;
-            vec_energy<MX>(acc, 0, cls1, double(e_dep), words);
+            vec_energy<R, MX>(acc, 0, cls1, e_dep, words);
             if (!counted) {
-                vec_energy<MX>(acc, 1, cls1, double(E), words);
+                vec_energy<R, MX>(acc, 1, cls1, E, words);
                 count1(acc + 24 + cls1);
                 ++words;
             }
@@ -187,37 +211,37 @@ __device__ __noinline__ void score_tallies(const RunParams& P, const V3<R>& p0, 
             continue;
         }
         // SurfaceTally::willPassThrough (surface_tally.cpp:16-34)
-        V3<R> nrm = {R(T.norm[0]), R(T.norm[1]), R(T.norm[2])};
+        V3<R> nrm = {pickr<R>(T.norm[0], T.fnorm[0]), pickr<R>(T.norm[1], T.fnorm[1]), pickr<R>(T.norm[2], T.fnorm[2])};
         R ec = dot(d, nrm);
         if (fabs_(ec) < R(kEps) || ec < R(0)) continue;
-        V3<R> a = {R(T.a[0]), R(T.a[1]), R(T.a[2])};
+        V3<R> a = {pickr<R>(T.a[0], T.fa[0]), pickr<R>(T.a[1], T.fa[1]), pickr<R>(T.a[2], T.fa[2])};
         V3<R> w = {a.x - p0.x, a.y - p0.y, a.z - p0.z};
         R t = dot(w, nrm) / ec;
         if (t > s || t < R(0)) continue;
         V3<R> ip = {p0.x + t * d.x, p0.y + t * d.y, p0.z + t * d.z};
         V3<R> rel = {ip.x - a.x, ip.y - a.y, ip.z - a.z};
         if (kind == MIDSX_TALLY_SURFACE_DISC) {
-            if (sqrt_(dot(rel, rel)) > R(T.radius)) continue;
+            if (sqrt_(dot(rel, rel)) > pickr<R>(T.radius, T.fradius)) continue;
         } else {
-            V3<R> e1 = {R(T.b[0]), R(T.b[1]), R(T.b[2])};
-            V3<R> e2 = {R(T.c[0]), R(T.c[1]), R(T.c[2])};
+            V3<R> e1 = {pickr<R>(T.b[0], T.fb[0]), pickr<R>(T.b[1], T.fb[1]), pickr<R>(T.b[2], T.fb[2])};
+            V3<R> e2 = {pickr<R>(T.c[0], T.fc[0]), pickr<R>(T.c[1], T.fc[1]), pickr<R>(T.c[2], T.fc[2])};
             R u = dot(e1, rel), v = dot(e2, rel);
-            if (u < R(0) || u > R(T.e1e1) || v < R(0) || v > R(T.e2e2)) continue;
+            if (u < R(0) || u > pickr<R>(T.e1e1, T.fe1e1) || v < R(0) || v > pickr<R>(T.e2e2, T.fe2e2)) continue;
             if (kind == MIDSX_TALLY_SURFACE_BINNED_RECT) {
-                int iu = int(u / R(T.e1e1) * R(T.nu));
-                int iv = int(v / R(T.e2e2) * R(T.nv));
+                int iu = int(u / pickr<R>(T.e1e1, T.fe1e1) * R(T.nu));
+                int iv = int(v / pickr<R>(T.e2e2, T.fe2e2) * R(T.nv));
                 iu = iu >= T.nu ? T.nu - 1 : iu;
                 iv = iv >= T.nv ? T.nv - 1 : iv;
                 unsigned long long* bin = T.acc + (size_t(iv) * T.nu + iu) * 8 + cls0 * 2;
-                Acc<MX>::energy(bin, double(E));
+                Acc<MX>::energy(bin, E);
                 count1(bin + 1);
                 ++words;
                 continue;
             }
         }
         unsigned long long* acc = T.acc;
-        vec_energy<MX>(acc, 0, cls0, double(E), words);
-        vec_cosine<MX>(acc, 1, cls0, double(ec), words);
+        vec_energy<R, MX>(acc, 0, cls0, E, words);
+        vec_cosine<R, MX>(acc, 1, cls0, ec, words);
         count1(acc + 24 + cls0);
         ++words;
     }
@@ -225,13 +249,23 @@ __device__ __noinline__ void score_tallies(const RunParams& P, const V3<R>& p0, 
 
 // ------------------------------------------------------------------ source sampling ---
 // PhotonSource::generatePhoton: position (PointGeometry), direction, energy, in that order.
+// The FP32 form reads the source's FP32 copies (no double-precision instruction on the path).
 template <typename R>
-__device__ void sample_source(const DevSource& S, HistoryRng& rng, V3<R>& pos, V3<R>& dir, R& E) {
-    pos = {R(S.pos[0]), R(S.pos[1]), R(S.pos[2])};
+__device__ __forceinline__ V3<R> src3(const double* d, const float* f) {
+    if constexpr (sizeof(R) == 8)
+        return {d[0], d[1], d[2]};
+    else
+        return {f[0], f[1], f[2]};
+}
+
+template <typename R>
+__device__ __noinline__ void sample_source(const DevSource& S, HistoryRng& rng, V3<R>& pos, V3<R>& dir, R& E) {
+    pos = src3<R>(S.pos, S.f_pos);
+    const V3<R> A = src3<R>(S.a, S.f_a), B = src3<R>(S.b, S.f_b), Cc = src3<R>(S.c, S.f_c);
     V3<R> d;
     switch (S.dir_kind) {
         case MIDSX_DIR_BEAM:
-            d = {R(S.a[0]) - pos.x, R(S.a[1]) - pos.y, R(S.a[2]) - pos.z};
+            d = {A.x - pos.x, A.y - pos.y, A.z - pos.z};
             break;
         case MIDSX_DIR_ISOTROPIC: {
             R theta = R(kPi) * uniform<R>(rng);
@@ -245,32 +279,45 @@ __device__ void sample_source(const DevSource& S, HistoryRng& rng, V3<R>& pos, V
         case MIDSX_DIR_RECTANGLE: {
             R a1 = uniform<R>(rng);
             R a2 = uniform<R>(rng);
-            d = {R(S.a[0]) + a1 * R(S.b[0]) + a2 * R(S.c[0]) - pos.x,
-                 R(S.a[1]) + a1 * R(S.b[1]) + a2 * R(S.c[1]) - pos.y,
-                 R(S.a[2]) + a1 * R(S.b[2]) + a2 * R(S.c[2]) - pos.z};
+            d = {A.x + a1 * B.x + a2 * Cc.x - pos.x, A.y + a1 * B.y + a2 * Cc.y - pos.y,
+                 A.z + a1 * B.z + a2 * Cc.z - pos.z};
             break;
         }
         default: {  // DISC
             R theta = R(2 * kPi) * uniform<R>(rng);
-            R r = R(S.radius) * uniform<R>(rng);
+            R radius;
+            if constexpr (sizeof(R) == 8)
+                radius = S.radius;
+            else
+                radius = S.f_radius;
+            R r = radius * uniform<R>(rng);
             R st, ct;
             sincos_(theta, &st, &ct);
-            d = {R(S.a[0]) + r * (R(S.b[0]) * ct + R(S.c[0]) * st) - pos.x,
-                 R(S.a[1]) + r * (R(S.b[1]) * ct + R(S.c[1]) * st) - pos.y,
-                 R(S.a[2]) + r * (R(S.b[2]) * ct + R(S.c[2]) * st) - pos.z};
+            d = {A.x + r * (B.x * ct + Cc.x * st) - pos.x, A.y + r * (B.y * ct + Cc.y * st) - pos.y,
+                 A.z + r * (B.z * ct + Cc.z * st) - pos.z};
             break;
         }
     }
     R nd = sqrt_(dot(d, d));
     dir = {d.x / nd, d.y / nd, d.z / nd};
     if (S.spec_kind == MIDSX_SPEC_MONO) {
-        E = R(S.mono);
+        if constexpr (sizeof(R) == 8)
+            E = S.mono;
+        else
+            E = S.f_mono;
     } else {
         // DiscreteInversion::sample: energy[lower_bound(cdf, U)], clamped to the last bin
-        double u = double(uniform<R>(rng));
-        int idx = lower_index(S.cdf, 0, S.n_bins, u);
+        const R u = uniform<R>(rng);
+        int idx;
+        if constexpr (sizeof(R) == 8)
+            idx = lower_index(S.cdf, 0, S.n_bins, u);
+        else
+            idx = lower_index(S.f_cdf, 0, S.n_bins, u);
         if (idx >= S.n_bins) idx = S.n_bins - 1;
-        E = R(S.energy[idx]);
+        if constexpr (sizeof(R) == 8)
+            E = S.energy[idx];
+        else
+            E = S.f_energy[idx];
     }
 }
 
@@ -381,6 +428,7 @@ struct midsx_gpu_phantom {
     DevGeom G;
     uint8_t* ids = nullptr;
     size_t n_voxels = 0;
+    const midsx_gpu_tables* tables = nullptr;  // the tables its dense material indices refer to
 };
 
 struct midsx_gpu_source {
@@ -452,6 +500,8 @@ void fill_spline(DevSpline& o, const midsx_spline_table& t) {
     o.degree = t.degree;
     o.lx_min = t.lx_min;
     o.lx_max = t.lx_max;
+    o.f_lx_min = float(t.lx_min);
+    o.f_lx_max = float(t.lx_max);
 }
 
 constexpr int kScalarWords = MIDSX_SCALAR_SLOTS;
@@ -557,6 +607,7 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
     T.rows = h->rows;
     T.n_materials = blob->n_materials;
     T.alpha = kMec2 / (std::sqrt(2.0) * 4.135667662e-15 * 299792458E2 * 1E8);
+    T.alpha_f = float(T.alpha);
     T.e_max = blob->e_max;
     fill_lin(T.majorant, blob->majorant);
     for (int m = 0; m < blob->n_materials; ++m) {
@@ -670,6 +721,7 @@ extern "C" midsx_status midsx_gpu_phantom_create(midsx_tables_h tables, const mi
     }
     G.background = bg;
     G.ids = p->ids;
+    p->tables = tables;
     *out = p;
     return MIDSX_OK;
 }
@@ -754,11 +806,18 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
             h[nb + i] = acc;
             s->max_energy = std::max(s->max_energy, spec->bin_energy[i]);
         }
-        CUDA_TRY(cudaMalloc(&s->buf, h.size() * sizeof(double)));
+        // device buffer: FP64 energies and CDF, then their FP32 copies
+        std::vector<float> hf(2 * size_t(nb));
+        for (size_t i = 0; i < hf.size(); ++i) hf[i] = float(h[i]);
+        CUDA_TRY(cudaMalloc(&s->buf, h.size() * sizeof(double) + hf.size() * sizeof(float)));
         CUDA_TRY(cudaMemcpy(s->buf, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        float* fbuf = reinterpret_cast<float*>(s->buf + h.size());
+        CUDA_TRY(cudaMemcpy(fbuf, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice));
         S.n_bins = nb;
         S.energy = s->buf;
         S.cdf = s->buf + nb;
+        S.f_energy = fbuf;
+        S.f_cdf = fbuf + nb;
     } else {
         if (!(spec->mono_energy > 0)) {
             delete s;
@@ -767,6 +826,14 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
         }
         s->max_energy = spec->mono_energy;
     }
+    for (int i = 0; i < 3; ++i) {
+        S.f_pos[i] = float(S.pos[i]);
+        S.f_a[i] = float(S.a[i]);
+        S.f_b[i] = float(S.b[i]);
+        S.f_c[i] = float(S.c[i]);
+    }
+    S.f_radius = float(S.radius);
+    S.f_mono = float(S.mono);
     *out = s;
     return MIDSX_OK;
 }
@@ -828,12 +895,22 @@ extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const 
             set_last_error("unknown tally kind");
             return MIDSX_INVALID_ARG;
         }
+        for (int k = 0; k < 3; ++k) {
+            d.fa[k] = float(d.a[k]);
+            d.fb[k] = float(d.b[k]);
+            d.fc[k] = float(d.c[k]);
+            d.fnorm[k] = float(d.norm[k]);
+        }
+        d.fradius = float(d.radius);
+        d.fe1e1 = float(d.e1e1);
+        d.fe2e2 = float(d.e2e2);
         d.acc = reinterpret_cast<unsigned long long*>(words);  // offset, fixed below
         words += (s.kind == MIDSX_TALLY_SURFACE_BINNED_RECT) ? size_t(s.nu) * s.nv * 8 : kScalarWords;
         t->host_specs.push_back(d);
     }
     t->acc_words = words;
-    if (!cuda_ok(cudaMalloc(&t->stats, kStCount * sizeof(unsigned long long)), "cudaMalloc") ||
+    // run statistics plus one word: the launch's history counter
+    if (!cuda_ok(cudaMalloc(&t->stats, (kStCount + 1) * sizeof(unsigned long long)), "cudaMalloc") ||
         (words && !cuda_ok(cudaMalloc(&t->acc, words * 8), "cudaMalloc")) ||
         (n_specs && !cuda_ok(cudaMalloc(&t->specs, n_specs * sizeof(DevTally)), "cudaMalloc")) ||
         (t->dose_stride &&
@@ -873,6 +950,60 @@ extern "C" midsx_status midsx_gpu_tallies_reset(midsx_tallies_h t, void* stream)
 
 namespace {
 
+void fill_job(DevJob& J, midsx_phantom_h phantom, midsx_source_h source, midsx_tallies_h tallies, uint64_t seed,
+              uint64_t first, uint64_t n) {
+    J.G = phantom->G;
+    J.S = source->S;
+    J.tallies = tallies->specs;
+    J.n_tallies = int(tallies->host_specs.size());
+    J.dose_stride = tallies->dose_stride;
+    J.dose = tallies->dose;
+    J.stats = tallies->stats;
+    J.seed = seed;
+    J.first = first;
+    J.n = n;
+}
+
+template <typename R, bool MULTI>
+midsx_status launch_typed(midsx_tables_h tables, const RunParams& P, const midsx_run_config& cfg, int block,
+                          cudaStream_t s) {
+    const size_t smem = kernel_smem<R>(P.n_jobs, MULTI, tables->T.n_materials, block);
+    if (smem > 48 * 1024)
+        CUDA_TRY(cudaFuncSetAttribute(transport_kernel<R, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(smem)));
+    int per_sm = cfg.blocks_per_sm;
+    if (per_sm <= 0) {
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<R, MULTI>, block, smem));
+        per_sm = std::max(per_sm, 1);
+    }
+    uint64_t want = (P.total + block - 1) / block;
+    uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(tables->sm_count) * per_sm));
+    transport_kernel<R, MULTI><<<unsigned(grid), block, smem, s>>>(P);
+    CUDA_TRY(cudaGetLastError());
+    return MIDSX_OK;
+}
+
+// Completes the launch parameters from cfg, zeroes the history counter and launches.
+midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_config& cfg, bool multi,
+                           void* stream) {
+    P.max_steps = cfg.max_steps > 0 ? cfg.max_steps : 100000;
+    P.max_trials = cfg.max_compton_trials > 0 ? cfg.max_compton_trials : 100000;
+    P.regroup = cfg.regroup > 0 ? std::min(cfg.regroup, 32) : 24;
+    P.chunk = cfg.chunk > 0 ? std::min(cfg.chunk, 64) : 1;
+    const bool mixed = cfg.precision == MIDSX_PREC_MIXED;
+    int block = cfg.block_size > 0 ? cfg.block_size : 256;
+    if (block > 256 || block % 32) {
+        set_last_error("block_size must be a multiple of 32 up to 256");
+        return MIDSX_INVALID_ARG;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), s));
+    if (mixed) return multi ? launch_typed<float, true>(tables, P, cfg, block, s)
+                            : launch_typed<float, false>(tables, P, cfg, block, s);
+    return multi ? launch_typed<double, true>(tables, P, cfg, block, s)
+                 : launch_typed<double, false>(tables, P, cfg, block, s);
+}
+
 midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_source_h source,
                         midsx_tallies_h tallies, const midsx_run_config* cfg, void* stream,
                         double* trace = nullptr) {
@@ -889,59 +1020,30 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
         set_last_error("dose tally size differs from the phantom");
         return MIDSX_INVALID_ARG;
     }
+    if (phantom->tables != tables) {
+        set_last_error("the phantom was created with other tables");
+        return MIDSX_INVALID_ARG;
+    }
     if (source->max_energy > tables->T.e_max) {
         set_last_error("source energy above the tables' e_max");
         return MIDSX_TABLE_RANGE;
+    }
+    if (cfg->precision == MIDSX_PREC_MIXED && source->max_energy > kMixedMaxEnergy) {
+        set_last_error("the mixed form's fixed-point tallies take source energies up to 262144 eV");
+        return MIDSX_INVALID_ARG;
     }
     if (cfg->n_histories == 0) return MIDSX_OK;
     RunParams P;
     std::memset(&P, 0, sizeof(P));
     P.T = tables->T;
-    P.G = phantom->G;
-    P.S = source->S;
-    P.tallies = tallies->specs;
-    P.n_tallies = int(tallies->host_specs.size());
-    P.dose_stride = tallies->dose_stride;
-    P.dose = tallies->dose;
-    P.stats = tallies->stats;
-    P.seed = cfg->seed;
-    P.first = cfg->first_history;
-    P.n = cfg->n_histories;
-    P.max_steps = cfg->max_steps > 0 ? cfg->max_steps : 100000;
-    P.max_trials = cfg->max_compton_trials > 0 ? cfg->max_compton_trials : 100000;
+    fill_job(P.job0, phantom, source, tallies, cfg->seed, cfg->first_history, cfg->n_histories);
+    P.n_jobs = 1;
+    P.counter = tallies->stats + kStCount;
+    P.total = cfg->n_histories;
     P.trace = trace;
-    P.regroup = cfg->regroup > 0 ? std::min(cfg->regroup, 32) : 16;
-    const bool mixed = cfg->precision == MIDSX_PREC_MIXED;
-    int block = cfg->block_size > 0 ? cfg->block_size : 256;
-    if (block > 256 || block % 32) {
-        set_last_error("block_size must be a multiple of 32 up to 256");
-        return MIDSX_INVALID_ARG;
-    }
-    size_t smem = size_t(2) * tables->T.n_materials * block * (mixed ? 4 : 8);
-    if (smem > 48 * 1024) {
-        if (mixed)
-            CUDA_TRY(cudaFuncSetAttribute(transport_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        else
-            CUDA_TRY(cudaFuncSetAttribute(transport_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    }
-    int per_sm = cfg->blocks_per_sm;
-    if (per_sm <= 0) {
-        if (mixed)
-            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<float>, block, smem));
-        else
-            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<double>, block, smem));
-        per_sm = std::max(per_sm, 1);
-    }
-    uint64_t want = (P.n + block - 1) / block;
-    uint64_t grid = std::min<uint64_t>(want, uint64_t(tables->sm_count) * per_sm);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (mixed)
-        transport_kernel<float><<<unsigned(grid), block, smem, s>>>(P);
-    else
-        transport_kernel<double><<<unsigned(grid), block, smem, s>>>(P);
-    CUDA_TRY(cudaGetLastError());
-    tallies->precision = cfg->precision;
-    return MIDSX_OK;
+    midsx_status st = launch_kernel(tables, P, *cfg, false, stream);
+    if (st == MIDSX_OK) tallies->precision = cfg->precision;
+    return st;
 }
 
 double fx_signed(unsigned long long v, double scale) { return double((long long)v) / scale; }
@@ -1131,7 +1233,8 @@ extern "C" midsx_status midsx_gpu_trace_deposits(midsx_tables_h tables, midsx_ph
 namespace {
 constexpr uint64_t kNoAllocMaxHistories = uint64_t(1) << 20;  // 1,048,576 histories, 8 MiB
 constexpr size_t kNoAllocStatsBytes = 256;
-static_assert(kStCount * sizeof(unsigned long long) <= kNoAllocStatsBytes, "statistics fit the scratch header");
+static_assert((kStCount + 1) * sizeof(unsigned long long) <= kNoAllocStatsBytes,
+              "statistics and the history counter fit the scratch header");
 }  // namespace
 
 static __device__ __align__(256) unsigned char midsx_noalloc_scratch[kNoAllocStatsBytes +
@@ -1238,3 +1341,260 @@ extern "C" midsx_status midsx_gpu_table_index(midsx_tables_h tables, int32_t mat
     cudaFree(di);
     return MIDSX_OK;
 }
+
+// ================================================================== batched launches ===
+struct midsx_gpu_batch {
+    midsx_tables_h tables = nullptr;
+    int n_jobs = 0;
+    std::vector<DevJob> host_jobs;
+    std::vector<unsigned long long> host_prefix;
+    std::vector<midsx_tallies_h> tallies;
+    DevJob* jobs = nullptr;
+    unsigned long long* prefix = nullptr;
+    unsigned long long* words = nullptr;  // [0] history counter, [1] epoch
+    cudaGraphExec_t graph = nullptr;
+    int graph_precision = -1;
+    double max_energy = 0;
+};
+
+namespace {
+
+void batch_params(const midsx_gpu_batch* b, RunParams& P, const unsigned long long* prefix, unsigned long long total) {
+    std::memset(&P, 0, sizeof(P));
+    P.T = b->tables->T;
+    P.jobs = b->jobs;
+    P.n_jobs = b->n_jobs;
+    P.prefix = prefix;
+    P.counter = b->words;
+    P.total = total;
+    P.epoch = b->words + 1;
+}
+
+midsx_status batch_check_precision(midsx_gpu_batch* b, int precision) {
+    if (precision != MIDSX_PREC_FP64 && precision != MIDSX_PREC_MIXED) {
+        set_last_error("unknown precision");
+        return MIDSX_INVALID_ARG;
+    }
+    if (precision == MIDSX_PREC_MIXED && b->max_energy > kMixedMaxEnergy) {
+        set_last_error("the mixed form's fixed-point tallies take source energies up to 262144 eV");
+        return MIDSX_INVALID_ARG;
+    }
+    for (auto* t : b->tallies) {
+        if (t->precision >= 0 && t->precision != precision) {
+            set_last_error("a job's tallies hold results of the other precision; reset them first");
+            return MIDSX_INVALID_ARG;
+        }
+    }
+    return MIDSX_OK;
+}
+
+// One batched launch followed by the epoch advance (both on `s`).
+midsx_status batch_enqueue(midsx_gpu_batch* b, const midsx_run_config& cfg, cudaStream_t s) {
+    RunParams P;
+    batch_params(b, P, b->prefix, b->host_prefix.back());
+    if (P.total == 0) return MIDSX_OK;
+    midsx_status st = launch_kernel(b->tables, P, cfg, true, s);
+    if (st != MIDSX_OK) return st;
+    advance_epoch_kernel<<<1, 1, 0, s>>>(b->words + 1);
+    CUDA_TRY(cudaGetLastError());
+    return MIDSX_OK;
+}
+
+}  // namespace
+
+extern "C" midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const midsx_batch_job* jobs, int32_t n_jobs,
+                                               midsx_batch_h* out) {
+    if (!tables || !jobs || !out || n_jobs < 1 || n_jobs > MIDSX_MAX_BATCH_JOBS) {
+        set_last_error("midsx_gpu_batch_create: invalid argument (1..64 jobs)");
+        return MIDSX_INVALID_ARG;
+    }
+    auto* b = new midsx_gpu_batch();
+    b->tables = tables;
+    b->n_jobs = n_jobs;
+    b->host_prefix.push_back(0);
+    for (int i = 0; i < n_jobs; ++i) {
+        const midsx_batch_job& j = jobs[i];
+        if (!j.phantom || !j.source || !j.tallies || j.phantom->tables != tables) {
+            delete b;
+            set_last_error("batch job " + std::to_string(i) + ": missing handle or phantom made with other tables");
+            return MIDSX_INVALID_ARG;
+        }
+        if (j.tallies->dose && j.tallies->n_voxels != j.phantom->n_voxels) {
+            delete b;
+            set_last_error("batch job " + std::to_string(i) + ": dose tally size differs from the phantom");
+            return MIDSX_INVALID_ARG;
+        }
+        if (j.source->max_energy > tables->T.e_max) {
+            delete b;
+            set_last_error("batch job " + std::to_string(i) + ": source energy above the tables' e_max");
+            return MIDSX_TABLE_RANGE;
+        }
+        DevJob d;
+        std::memset(&d, 0, sizeof(d));
+        fill_job(d, j.phantom, j.source, j.tallies, j.seed, j.first_history, j.n_histories);
+        b->host_jobs.push_back(d);
+        b->tallies.push_back(j.tallies);
+        b->host_prefix.push_back(b->host_prefix.back() + j.n_histories);
+        b->max_energy = std::max(b->max_energy, j.source->max_energy);
+    }
+    if (!cuda_ok(cudaMalloc(&b->jobs, n_jobs * sizeof(DevJob)), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&b->prefix, (n_jobs + 1) * sizeof(unsigned long long)), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&b->words, 2 * sizeof(unsigned long long)), "cudaMalloc")) {
+        midsx_gpu_batch_destroy(b);
+        return MIDSX_OOM;
+    }
+    CUDA_TRY(cudaMemcpy(b->jobs, b->host_jobs.data(), n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(b->prefix, b->host_prefix.data(), (n_jobs + 1) * sizeof(unsigned long long),
+                        cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(b->words, 0, 2 * sizeof(unsigned long long)));
+    *out = b;
+    return MIDSX_OK;
+}
+
+extern "C" midsx_status midsx_gpu_batch_destroy(midsx_batch_h b) {
+    if (!b) return MIDSX_INVALID_ARG;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    cudaFree(b->jobs);
+    cudaFree(b->prefix);
+    cudaFree(b->words);
+    delete b;
+    return MIDSX_OK;
+}
+
+extern "C" midsx_status midsx_gpu_batch_run(midsx_batch_h b, const midsx_run_config* cfg, void* stream) {
+    if (!b || !cfg) return MIDSX_INVALID_ARG;
+    midsx_status st = batch_check_precision(b, cfg->precision);
+    if (st != MIDSX_OK) return st;
+    st = batch_enqueue(b, *cfg, static_cast<cudaStream_t>(stream));
+    if (st == MIDSX_OK)
+        for (auto* t : b->tallies) t->precision = cfg->precision;
+    return st;
+}
+
+extern "C" midsx_status midsx_gpu_batch_capture(midsx_batch_h b, const midsx_run_config* cfg, void* stream) {
+    if (!b || !cfg || !stream) {
+        set_last_error("midsx_gpu_batch_capture needs a non-default stream");
+        return MIDSX_INVALID_ARG;
+    }
+    midsx_status st = batch_check_precision(b, cfg->precision);
+    if (st != MIDSX_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // attributes and occupancy are resolved outside the capture
+    RunParams P;
+    batch_params(b, P, b->prefix, b->host_prefix.back());
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    midsx_status enq = batch_enqueue(b, *cfg, s);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (enq != MIDSX_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return enq;
+    }
+    if (!cuda_ok(e, "cudaStreamEndCapture")) return MIDSX_CUDA_ERROR;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (!cuda_ok(e, "cudaGraphInstantiate")) return MIDSX_CUDA_ERROR;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = exec;
+    b->graph_precision = cfg->precision;
+    return MIDSX_OK;
+}
+
+extern "C" midsx_status midsx_gpu_batch_replay(midsx_batch_h b, void* stream) {
+    if (!b || !b->graph) {
+        set_last_error("no captured graph");
+        return MIDSX_INVALID_ARG;
+    }
+    midsx_status st = batch_check_precision(b, b->graph_precision);
+    if (st != MIDSX_OK) return st;
+    CUDA_TRY(cudaGraphLaunch(b->graph, static_cast<cudaStream_t>(stream)));
+    for (auto* t : b->tallies) t->precision = b->graph_precision;
+    return MIDSX_OK;
+}
+
+extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precision, uint64_t trial_histories,
+                                                 midsx_run_config* best, double* best_rate, void* stream) {
+    if (!b || !best || trial_histories < 1000) return MIDSX_INVALID_ARG;
+    midsx_status st = batch_check_precision(b, precision);
+    if (st != MIDSX_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // trial prefix: every job contributes in proportion to its size (at least one history)
+    const double total = double(b->host_prefix.back());
+    std::vector<unsigned long long> tp(1, 0);
+    for (int i = 0; i < b->n_jobs; ++i) {
+        double share = total > 0 ? double(b->host_jobs[size_t(i)].n) / total : 1.0 / b->n_jobs;
+        unsigned long long k = std::max<unsigned long long>(1, (unsigned long long)(share * double(trial_histories)));
+        tp.push_back(tp.back() + k);
+    }
+    unsigned long long* dprefix = nullptr;
+    CUDA_TRY(cudaMalloc(&dprefix, tp.size() * sizeof(unsigned long long)));
+    CUDA_TRY(cudaMemcpy(dprefix, tp.data(), tp.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    const int blocks[] = {128, 256};
+    const int per_sms[] = {0, 2, 4};
+    const int regroups[] = {12, 16, 20, 24, 28};
+    const int chunks[] = {1, 4};
+    double best_r = -1;
+    midsx_run_config cand;
+    std::memset(&cand, 0, sizeof(cand));
+    cand.precision = precision;
+    RunParams P;
+    batch_params(b, P, dprefix, tp.back());
+    for (int pass = 0; pass < 2 && st == MIDSX_OK; ++pass) {  // pass 0 warms the caches
+        for (int bs : blocks)
+            for (int ps : per_sms)
+                for (int rg : regroups)
+                    for (int ch : chunks) {
+                        if (st != MIDSX_OK) break;
+                        cand.block_size = bs;
+                        cand.blocks_per_sm = ps;
+                        cand.regroup = rg;
+                        cand.chunk = ch;
+                        if (!cuda_ok(cudaEventRecord(e0, s), "cudaEventRecord")) st = MIDSX_CUDA_ERROR;
+                        if (st == MIDSX_OK) st = launch_kernel(b->tables, P, cand, true, s);
+                        if (st == MIDSX_OK && !cuda_ok(cudaEventRecord(e1, s), "cudaEventRecord")) st = MIDSX_CUDA_ERROR;
+                        if (st == MIDSX_OK) st = wait_stream(stream);
+                        float ms = 0;
+                        if (st == MIDSX_OK && !cuda_ok(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime"))
+                            st = MIDSX_CUDA_ERROR;
+                        if (st == MIDSX_OK && pass == 1 && ms > 0) {
+                            double r = double(tp.back()) / (ms * 1e-3);
+                            if (r > best_r) {
+                                best_r = r;
+                                *best = cand;
+                            }
+                        }
+                        if (pass == 0) break;  // one warm-up launch per block size is enough
+                    }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(dprefix);
+    if (st != MIDSX_OK) return st;
+    for (auto* t : b->tallies) {
+        st = midsx_gpu_tallies_reset(t, stream);
+        if (st != MIDSX_OK) return st;
+    }
+    if (best_rate) *best_rate = best_r;
+    return wait_stream(stream);
+}
+
+// ==================================================================== stream helpers ===
+extern "C" midsx_status midsx_gpu_stream_create(void** stream_out) {
+    if (!stream_out) return MIDSX_INVALID_ARG;
+    cudaStream_t s = nullptr;
+    CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    *stream_out = s;
+    return MIDSX_OK;
+}
+
+extern "C" midsx_status midsx_gpu_stream_destroy(void* stream) {
+    if (!stream) return MIDSX_INVALID_ARG;
+    CUDA_TRY(cudaStreamDestroy(static_cast<cudaStream_t>(stream)));
+    return MIDSX_OK;
+}
+
+extern "C" midsx_status midsx_gpu_stream_synchronize(void* stream) { return wait_stream(stream); }

@@ -76,8 +76,14 @@ class TallySpec(C.Structure):
 class RunConfig(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_steps", C.c_int32),
                 ("max_compton_trials", C.c_int32), ("block_size", C.c_int32),
-                ("blocks_per_sm", C.c_int32), ("regroup", C.c_int32), ("seed", C.c_uint64),
+                ("blocks_per_sm", C.c_int32), ("regroup", C.c_int32), ("chunk", C.c_int32),
+                ("reserved", C.c_int32), ("seed", C.c_uint64),
                 ("first_history", C.c_uint64), ("n_histories", C.c_uint64)]
+
+
+class BatchJob(C.Structure):
+    _fields_ = [("phantom", C.c_void_p), ("source", C.c_void_p), ("tallies", C.c_void_p),
+                ("seed", C.c_uint64), ("first_history", C.c_uint64), ("n_histories", C.c_uint64)]
 
 
 class RunStats(C.Structure):
@@ -124,6 +130,15 @@ _SIGNATURES = {
     "midsx_gpu_sample": (C.c_int, [VP, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64,
                                    C.c_uint64, C.c_int64, PD, PD]),
     "midsx_gpu_table_index": (C.c_int, [VP, C.c_int32, PD, C.c_int64, PI64]),
+    "midsx_gpu_stream_create": (C.c_int, [C.POINTER(VP)]),
+    "midsx_gpu_stream_destroy": (C.c_int, [VP]),
+    "midsx_gpu_stream_synchronize": (C.c_int, [VP]),
+    "midsx_gpu_batch_create": (C.c_int, [VP, C.POINTER(BatchJob), C.c_int32, C.POINTER(VP)]),
+    "midsx_gpu_batch_destroy": (C.c_int, [VP]),
+    "midsx_gpu_batch_run": (C.c_int, [VP, C.POINTER(RunConfig), VP]),
+    "midsx_gpu_batch_capture": (C.c_int, [VP, C.POINTER(RunConfig), VP]),
+    "midsx_gpu_batch_replay": (C.c_int, [VP, VP]),
+    "midsx_gpu_batch_autotune": (C.c_int, [VP, C.c_int32, C.c_uint64, C.POINTER(RunConfig), PD, VP]),
     "midsx_gpu_trace_deposits": (C.c_int, [VP, VP, VP, C.POINTER(RunConfig), PD]),
     "midsx_gpu_trace_deposits_noalloc": (C.c_int, [VP, VP, VP, C.POINTER(RunConfig), PD, VP]),
 }

@@ -138,6 +138,32 @@ def cone_beam_dose(n_histories=100_000_000, shape=(128, 256, 256), spacing=0.05,
                  DOSE_FULL, n_histories, 150e3)
 
 
+def batch_jobs(n_jobs=64, seed=1, edge_range=(32, 256), kvp_range=(20.0, 120.0), hist_range=(1e5, 1e8),
+               hist_scale=1.0, spacing=0.1):
+    """The batched configuration: n_jobs independent simulations, phantom edge log-uniform in
+    edge_range voxels at `spacing` cm (seeded ellipsoid phantoms), Kramers spectra with kVp
+    uniform in kvp_range, history counts log-uniform in hist_range (times hist_scale), each
+    with its own per-voxel dose tally.  Returns a list of Scene."""
+    rng = np.random.default_rng(seed)
+    out = []
+    al = api.TableBlob([ALUMINIUM], e_max=150e3)
+    for j in range(n_jobs):
+        edge = int(round(np.exp(rng.uniform(np.log(edge_range[0]), np.log(edge_range[1])))))
+        kvp = float(np.round(rng.uniform(*kvp_range)))
+        n = int(np.exp(rng.uniform(np.log(hist_range[0]), np.log(hist_range[1]))) * hist_scale)
+        shape = (edge, edge, edge)
+        ids = ellipsoid_phantom(shape, spacing, seed=1000 + j, n_ellipsoids=max(4, edge // 8))
+        ext = edge * spacing
+        z0 = 10.0 + 0.5
+        domain = (ext, ext, z0 + ext + 1.0)
+        spectrum = kramers_spectrum(kvp, e_min=min(10.0, kvp - 5.0), tables=al)
+        source = dict(position=(ext / 2, ext / 2, 0.5), direction=("disc", (ext / 2, ext / 2, z0), (0, 0, 1), ext / 2),
+                      spectrum=spectrum)
+        out.append(Scene("batch_job_%d_%d^3_%gkVp" % (j, edge, kvp), [AIR, SOFT_TISSUE, ADIPOSE, CORTICAL_BONE],
+                         domain, (spacing,) * 3, (0.0, 0.0, z0), ids, AIR, source, [], DOSE_FULL, max(n, 1), 150e3))
+    return out
+
+
 def radiography(n_histories=1_000_000_000, shape=(256, 512, 512), spacing=0.05, seed=1, det_bins=512,
                 det_pitch=0.1, sid=100.0, kvp=100.0):
     nz, ny, nx = shape

@@ -1,0 +1,114 @@
+"""Batched launches: several simulations with different phantoms, sources, seeds and history
+counts in one persistent launch (midsx_gpu_batch_*), CUDA-graph capture and replay, and the
+launch-shape autotuner.  Each job's results must equal those of running that job alone on
+the same Philox streams: bit for bit in the mixed form (integer tallies), to rounding in FP64.
+"""
+import numpy as np
+import pytest
+
+import midsx_gb300 as M
+from midsx_gb300 import native as N
+from midsx_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    jobs = scenes.batch_jobs(n_jobs=4, seed=7, edge_range=(16, 40), hist_range=(2e4, 2e5), spacing=0.2)
+    tables = M.Tables(jobs[0].materials, e_max=150e3)
+    return tables, jobs
+
+
+def make(tables, sc):
+    ph = M.Phantom(tables, sc.domain, sc.spacing, sc.origin, sc.ids, sc.background)
+    src = M.Source(**sc.source)
+    tl = M.Tallies(ph, sc.specs, sc.dose_mode)
+    return ph, src, tl
+
+
+def results(tl):
+    d = tl.dose()
+    st = tl.stats()
+    return d["sum"].copy(), d["sumsq"].copy(), d["count"].copy(), st
+
+
+def test_batch_jobs_equal_single_runs(setup):
+    tables, jobs = setup
+    objs = [make(tables, sc) for sc in jobs]
+    batch = M.Batch(tables, [(ph, src, tl, 100 + j, 1000 * j, sc.n_histories)
+                             for j, (sc, (ph, src, tl)) in enumerate(zip(jobs, objs))])
+    batch.run("mixed")
+    for j, sc in enumerate(jobs):
+        ph, src, tl = make(tables, sc)
+        M.run(tables, ph, src, tl, sc.n_histories, seed=100 + j, first=1000 * j, precision="mixed")
+        a = results(objs[j][2])
+        b = results(tl)
+        for x, y in zip(a[:3], b[:3]):
+            np.testing.assert_array_equal(x, y)
+        for k in ("histories", "steps", "voxel_fetches", "photo", "coherent", "incoherent", "deposited_grid",
+                  "escaped_energy", "source_energy"):
+            assert a[3][k] == b[3][k], (j, k)
+        assert a[3]["histories"] == sc.n_histories
+
+
+def test_batch_fp64_equals_single_runs(setup):
+    tables, jobs = setup
+    objs = [make(tables, sc) for sc in jobs[:2]]
+    batch = M.Batch(tables, [(ph, src, tl, 5, 0, sc.n_histories) for sc, (ph, src, tl) in zip(jobs[:2], objs)])
+    batch.run("fp64")
+    for j, sc in enumerate(jobs[:2]):
+        ph, src, tl = make(tables, sc)
+        M.run(tables, ph, src, tl, sc.n_histories, seed=5, precision="fp64")
+        a, b = results(objs[j][2]), results(tl)
+        np.testing.assert_allclose(a[0], b[0], rtol=1e-9, atol=1e-6)
+        np.testing.assert_array_equal(a[2], b[2])
+        assert a[3]["steps"] == b[3]["steps"]
+
+
+def test_graph_replays_advance_epochs(setup):
+    """Two graph replays equal two batch runs and equal single runs over [first, first + 2n)."""
+    tables, jobs = setup
+    sub = jobs[:3]
+    stream = M.Stream()
+    A = [make(tables, sc) for sc in sub]
+    B = [make(tables, sc) for sc in sub]
+    ba = M.Batch(tables, [(ph, src, tl, 9, 0, sc.n_histories) for sc, (ph, src, tl) in zip(sub, A)])
+    bb = M.Batch(tables, [(ph, src, tl, 9, 0, sc.n_histories) for sc, (ph, src, tl) in zip(sub, B)])
+    ba.capture(stream.handle, "mixed", regroup=20)
+    ba.replay(stream.handle)
+    ba.replay(stream.handle)
+    stream.synchronize()
+    bb.run("mixed", stream.handle, regroup=12)
+    bb.run("mixed", stream.handle)
+    stream.synchronize()
+    for j, sc in enumerate(sub):
+        ph, src, tl = make(tables, sc)
+        M.run(tables, ph, src, tl, 2 * sc.n_histories, seed=9, precision="mixed")
+        a, b, c = results(A[j][2]), results(B[j][2]), results(tl)
+        for x, y, z in zip(a[:3], b[:3], c[:3]):
+            np.testing.assert_array_equal(x, y)
+            np.testing.assert_array_equal(x, z)
+        assert a[3]["histories"] == 2 * sc.n_histories
+
+
+def test_autotune_picks_a_shape_and_resets_tallies(setup):
+    tables, jobs = setup
+    objs = [make(tables, sc) for sc in jobs]
+    batch = M.Batch(tables, [(ph, src, tl, 1, 0, sc.n_histories) for sc, (ph, src, tl) in zip(jobs, objs)])
+    launch, rate = batch.autotune("mixed", trial=200_000)
+    assert rate > 0
+    assert launch["block"] in (128, 256) and 12 <= launch["regroup"] <= 28 and launch["chunk"] in (1, 4)
+    for ph, src, tl in objs:
+        assert tl.dose()["sum"].sum() == 0 and tl.stats()["histories"] == 0
+    batch.run("mixed", **launch)
+    assert sum(tl.stats()["histories"] for _, _, tl in objs) == batch.histories
+
+
+def test_batch_rejects_mismatched_tables(setup):
+    tables, jobs = setup
+    other = M.Tables(jobs[0].materials, e_max=150e3)
+    ph, src, tl = make(other, jobs[0])
+    with pytest.raises(N.MidsxError) as e:
+        M.Batch(tables, [(ph, src, tl, 1, 0, 10)])
+    assert e.value.status == N.INVALID_ARG
