@@ -37,7 +37,11 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--histories", type=float, default=1e8)
     p.add_argument("--cpu-sample", type=float, default=1e6, help="histories of the CPU baseline sample")
-    p.add_argument("--quick", action="store_true", help="skip the FP64, e2e and CPU legs")
+    p.add_argument("--quick", action="store_true", help="skip the FP64, e2e, CPU, batched and serving legs")
+    p.add_argument("--batched", type=int, default=1, help="run the 64-job batched leg (1/0)")
+    p.add_argument("--batch-scale", type=float, default=1.0, help="history scale of the batched jobs")
+    p.add_argument("--serving", type=int, default=1, help="run the serving leg (1/0)")
+    p.add_argument("--serving-requests", type=int, default=120, help="requests at 200/s in the serving leg")
     return p.parse_args()
 
 
@@ -298,7 +302,97 @@ def main():
                           "kernel_ms": 1e3 * kernel_s}
     if "e2e" not in result:
         result["e2e"] = None
+    if not args.quick and args.batched:
+        result["batched"] = batched_leg(args, torch)
+    if not args.quick and args.serving:
+        result["serving"] = serving_leg(args)
     print(json.dumps(result), flush=True)
+
+
+def batched_leg(args, torch):
+    """64 independent simulations (phantom edge log-uniform 32-256 voxels at 1 mm, 20-120 kVp,
+    1e5-1e8 histories each, own dose tallies) in one persistent launch: launch shape from the
+    autotuner, the launch captured in a CUDA graph and replayed; beside it the same jobs run
+    one midsx_gpu_run each, back to back on one stream."""
+    import midsx_gb300 as M
+    from midsx_gb300 import scenes
+    t0 = time.time()
+    jobs = scenes.batch_jobs(n_jobs=64, seed=1, hist_scale=args.batch_scale)
+    tables = M.Tables(jobs[0].materials, e_max=150e3)
+    objs = []
+    for sc in jobs:
+        ph = M.Phantom(tables, sc.domain, sc.spacing, sc.origin, sc.ids, sc.background)
+        objs.append((ph, M.Source(**sc.source), M.Tallies(ph, sc.specs, sc.dose_mode)))
+    log("batched setup %.1fs" % (time.time() - t0))
+    batch = M.Batch(tables, [(ph, src, tl, 1 + j, 0, sc.n_histories)
+                             for j, (sc, (ph, src, tl)) in enumerate(zip(jobs, objs))])
+    stream = M.Stream()
+    launch, tuned_rate = batch.autotune("mixed", trial=4_000_000, stream=stream.handle)
+    batch.capture(stream.handle, "mixed", **launch)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ts = torch.cuda.ExternalStream(stream.handle.value)
+    batch.replay(stream.handle)  # warm-up
+    stream.synchronize()
+    reps = 2
+    ev[0].record(ts)
+    for _ in range(reps):
+        batch.replay(stream.handle)
+    ev[1].record(ts)
+    stream.synchronize()
+    graph_s = ev[0].elapsed_time(ev[1]) / 1e3 / reps
+    # the same jobs as separate single-simulation launches
+    ev2 = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev2[0].record(ts)
+    for j, (sc, (ph, src, tl)) in enumerate(zip(jobs, objs)):
+        tl.reset(stream.handle)
+        M.run(tables, ph, src, tl, sc.n_histories, seed=1 + j, first=0, precision="mixed", stream=stream.handle,
+              **launch)
+    ev2[1].record(ts)
+    stream.synchronize()
+    seq_s = ev2[0].elapsed_time(ev2[1]) / 1e3
+    h = batch.histories
+    out = {"workload": "64 jobs, edge 32-256 voxels at 1 mm, 20-120 kVp, histories log-uniform 1e5-1e8 x %g"
+                       % args.batch_scale,
+           "histories_per_replay": h, "value": h / graph_s, "unit": UNIT, "ms_per_replay": 1e3 * graph_s,
+           "separate_launches_value": h / seq_s, "autotuned_launch": launch, "autotune_trial_rate": tuned_rate,
+           "replays_timed": reps}
+    batch.close()
+    stream.close()
+    return out
+
+
+def serving_leg(args):
+    """The serving mix (70% 64^3 dose 1e6, 25% 128^3 dose 1e7, 5% 256x256x128 radiography with
+    a 256^2 detector 1e8) as a seeded Poisson stream at 200 requests/s, then at 80% of the
+    request rate the server sustained."""
+    from midsx_gb300 import scenes, serving
+    t0 = time.time()
+    tmpl = scenes.serving_templates(pool=4, seed=1)
+    mix = serving.Mix(tmpl)
+    log("serving setup %.1fs" % (time.time() - t0))
+    # warm-up: one request of each class
+    warm = [dict(t=0.0, cls=c[0], template=0, n=200_000, seed=999 + k, first=0)
+            for k, c in enumerate(scenes.SERVING_CLASSES)]
+    serving.drive(mix, warm)
+    reqs = scenes.serving_requests(rate=200.0, n_requests=args.serving_requests, seed=1)
+    hot = serving.drive(mix, reqs)
+    mean_h = hot["histories"] / hot["requests"]
+    rate = max(1.0, 0.8 * hot["histories_per_s"] / mean_h)
+    reqs2 = scenes.serving_requests(rate=rate, n_requests=max(20, args.serving_requests // 2), seed=2)
+    calm = serving.drive(mix, reqs2)
+    mix.close()
+
+    def brief(d, lam):
+        s = d["server"]
+        return {"rate_req_per_s": lam, "requests": d["requests"], "failed": d["failed"],
+                "histories_per_s": d["histories_per_s"], "offered_histories_per_s": d["offered_histories_per_s"],
+                "latency_ms": d["latency_ms"], "server_latency_ms": d["server_latency_ms"],
+                "by_class": d["by_class"], "launches": s["launches"], "max_active": s["max_active_seen"],
+                "peak_hbm_bytes": s["peak_bytes_in_use"], "gpu_busy_s": s["busy_seconds"]}
+
+    return {"workload": "poisson mix: 70% 64^3 dose 1e6, 25% 128^3 dose 1e7, 5% 256x256x128 radiography "
+                        "256^2 detector 1e8 (mixed precision)",
+            "at_200_req_per_s": brief(hot, 200.0), "at_sustainable_rate": brief(calm, rate)}
 
 
 def _run_host(M, N, tables, geom, ids_pinned, src_spec, sc, cfg, dose_pinned):

@@ -337,6 +337,95 @@ midsx_status midsx_gpu_batch_replay(midsx_batch_h b, void* stream);
 midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precision, uint64_t trial_histories,
                                       midsx_run_config* best, double* best_rate, void* stream);
 
+/* ------------------------------------------------------------------ request server --- */
+/* A request loop on one GPU with continuous batching.  No reference counterpart (MIDSX runs
+ * one simulation per runSimulation call, src/MIDSX/Core/run_simulation.cpp:6-41).
+ *  - The tables and every registered phantom stay on the device across requests; a phantom
+ *    is evicted (least recently used, no request using it) only when an admission needs its
+ *    memory, and uploaded again from the server's host copy when a request needs it.
+ *  - A request names a registered phantom, a source handle (the caller's; it must outlive the
+ *    request), tally specs, a dose mode, a seed, a history range and a precision.  It is
+ *    admitted in arrival order when a job slot is free and its footprint (its tallies, plus
+ *    its phantom when that is not resident) fits the HBM budget.
+ *  - A scheduler thread keeps up to `launches_in_flight` batched launches queued on the GPU.
+ *    Each launch gives every admitted request with histories left a share of
+ *    `launch_histories` (equal shares, smaller requests take only what they need), so a
+ *    request that arrives while launches run joins the next launch.
+ *  - History ids, not launch boundaries, select the Philox streams: a request's results equal
+ *    those of a single midsx_gpu_run of the same phantom, source, tallies, seed and range -
+ *    bit for bit in the mixed form, to FP64 rounding order in the FP64 form.
+ * Calls are thread-safe.  Times are seconds on the server's monotonic clock. */
+typedef struct midsx_gpu_server* midsx_server_h;
+
+typedef struct midsx_server_config {
+    uint64_t hbm_budget_bytes;   /* phantoms + request tallies (0 = 90% of the free memory) */
+    uint64_t launch_histories;   /* histories per batched launch (0 = 4,000,000) */
+    int32_t max_active;          /* admitted requests, 1..64 (0 = 64) */
+    int32_t launches_in_flight;  /* 1..4 (0 = 2) */
+    midsx_run_config launch;     /* launch shape and caps; precision, seed and range unused */
+} midsx_server_config;
+
+typedef struct midsx_request {
+    int32_t phantom;                 /* id from midsx_server_add_phantom */
+    int32_t precision;               /* midsx_precision */
+    int32_t dose_mode;               /* midsx_dose_mode */
+    int32_t n_tallies;
+    const midsx_tally_spec* tallies; /* copied at submission */
+    midsx_source_h source;
+    uint64_t seed;
+    uint64_t first_history;
+    uint64_t n_histories;
+} midsx_request;
+
+typedef enum midsx_request_state {
+    MIDSX_REQ_QUEUED = 0,
+    MIDSX_REQ_RUNNING = 1,
+    MIDSX_REQ_DONE = 2,
+    MIDSX_REQ_FAILED = 3
+} midsx_request_state;
+
+typedef struct midsx_request_info {
+    int32_t state;               /* midsx_request_state */
+    int32_t status;              /* midsx_status of a failed request */
+    int32_t launches;            /* batched launches the request took part in */
+    int32_t reserved;
+    uint64_t histories_scheduled;
+    uint64_t histories_done;
+    uint64_t footprint_bytes;    /* device bytes charged at admission */
+    double t_submit, t_admit, t_first_launch, t_done;  /* -1 until reached */
+} midsx_request_info;
+
+typedef struct midsx_server_stats {
+    uint64_t submitted, admitted, completed, failed;
+    uint64_t launches, histories;
+    uint64_t budget_bytes, bytes_in_use, peak_bytes_in_use, resident_phantom_bytes;
+    uint64_t phantom_uploads, phantom_evictions;
+    int32_t queued, active, max_active_seen, reserved;
+    double busy_seconds;         /* sum of launch durations (device events) */
+} midsx_server_stats;
+
+midsx_status midsx_server_create(midsx_tables_h tables, const midsx_server_config* cfg, midsx_server_h* out);
+/* Stops the scheduler after the launches in flight, frees every request and phantom. */
+midsx_status midsx_server_destroy(midsx_server_h s);
+/* Registers a phantom with the tables its requests run with (NULL = the server's tables; the
+ * tables must outlive the server); synchronous.  Each launch runs requests of one (tables,
+ * precision) group: a phantom without lead need not take the lead-dominated majorant of
+ * another request.  The server keeps a host copy of the dense voxel grid for uploads after
+ * an eviction. */
+midsx_status midsx_server_add_phantom(midsx_server_h s, midsx_tables_h tables, const midsx_geometry_spec* geom,
+                                      const uint8_t* ids, int32_t* phantom_id);
+midsx_status midsx_server_submit(midsx_server_h s, const midsx_request* r, uint64_t* request_id);
+midsx_status midsx_server_poll(midsx_server_h s, uint64_t request_id, midsx_request_info* out);
+/* Waits until the request is done or failed, or timeout_s passes (MIDSX_TIMEOUT). */
+midsx_status midsx_server_wait(midsx_server_h s, uint64_t request_id, double timeout_s, midsx_request_info* out);
+/* The tallies of a done request, to read with midsx_gpu_fetch_*; valid until release.  They
+ * belong to the server: midsx_gpu_tallies_destroy refuses them. */
+midsx_status midsx_server_tallies(midsx_server_h s, uint64_t request_id, midsx_tallies_h* out);
+/* Returns a finished request's memory to the budget and forgets the request. */
+midsx_status midsx_server_release(midsx_server_h s, uint64_t request_id);
+midsx_status midsx_server_get_stats(midsx_server_h s, midsx_server_stats* out);
+midsx_status midsx_server_now(midsx_server_h s, double* t);
+
 /* ----------------------------------------------------------- sampler diagnostics --- */
 /* Draw n samples of one sampler on the device with the transport kernel's own device
  * functions and Philox streams (history id = first + i, draw counter from 0).  Used by the

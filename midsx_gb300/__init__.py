@@ -5,6 +5,6 @@ MIDSX (include/MIDSX/Core.h) by lib/libmidsx_core.so.  This package binds the C 
 Python callers, tests and the benchmark.
 """
 from . import build, native  # noqa: F401
-from .api import (DATA_DIR, Batch, Phantom, Source, Stream, Tables, TableBlob, Tallies,  # noqa: F401
+from .api import (DATA_DIR, Batch, Phantom, Server, Source, Stream, Tables, TableBlob, Tallies,  # noqa: F401
                   geometry_spec, material_id, material_name, run, run_config, run_host,
                   sample, source_spec, table_index, tally_specs, trace_deposits)

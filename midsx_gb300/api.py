@@ -231,6 +231,7 @@ class Tallies:
         self.specs = list(specs)
         self.dose_mode = dose_mode
         self.phantom = phantom
+        self.shape = phantom.ids.shape if phantom is not None else None
         arr = tally_specs(self.specs)
         lib = N.load()
         h = C.c_void_p()
@@ -249,14 +250,14 @@ class Tallies:
         return st.as_dict()
 
     def dose(self, stream=None):
-        n = self.phantom.n_voxels
+        n = int(np.prod(self.shape))
         s = np.empty(n)
         full = self.dose_mode == N.DOSE_FULL
         s2 = np.empty(n) if full else None
         c = np.empty(n) if full else None
         N.check(N.load().midsx_gpu_fetch_dose(self.handle, N.dptr(s), N.dptr(s2) if full else None,
                                               N.dptr(c) if full else None, stream), "midsx_gpu_fetch_dose")
-        shape = self.phantom.ids.shape
+        shape = self.shape
         out = {"sum": s.reshape(shape)}
         if full:
             out["sumsq"] = s2.reshape(shape)
@@ -427,3 +428,114 @@ def run_host(tables, geom_spec, ids, source_spec_, specs, dose_mode, cfg):
                                         N.dptr(dose) if dose is not None else None, C.byref(st)),
             "midsx_gpu_run_host")
     return dose, st.as_dict()
+
+
+class TallyView(Tallies):
+    """Read access to tallies another object owns (a request server's); closing it does
+    not free them."""
+
+    def __init__(self, handle, shape, specs=(), dose_mode=N.DOSE_FULL):
+        self.handle = handle
+        self.shape = shape
+        self.specs = list(specs)
+        self.dose_mode = dose_mode
+        self.phantom = None
+
+    def close(self):
+        self.handle = None
+
+
+class Server:
+    """Request server with continuous batching (midsx_server_*): phantoms registered once and
+    kept on the device, requests admitted by HBM footprint and advanced together in batched
+    launches by a native scheduler thread.  launch: launch shape (block, per_sm, regroup,
+    chunk, max_steps, max_trials)."""
+
+    def __init__(self, tables, budget_bytes=0, launch_histories=0, max_active=0, in_flight=0, **launch):
+        cfg = N.ServerConfig()
+        cfg.hbm_budget_bytes = int(budget_bytes)
+        cfg.launch_histories = int(launch_histories)
+        cfg.max_active = int(max_active)
+        cfg.launches_in_flight = int(in_flight)
+        cfg.launch = run_config(0, 0, 0, "mixed", **launch)
+        h = C.c_void_p()
+        N.check(N.load().midsx_server_create(tables.handle, C.byref(cfg), C.byref(h)), "midsx_server_create")
+        self.handle = h
+        self.tables = tables
+        self._tables = []  # tables of registered phantoms, kept alive with the server
+        self._shapes = {}
+        self._requests = {}  # id -> (source kept alive, specs, dose_mode, phantom id)
+
+    def add_phantom(self, domain, spacing, origin, ids, background_id, tables=None):
+        """Registers a phantom; its requests run with `tables` (default: the server's)."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint8)
+        nz, ny, nx = ids.shape
+        spec = geometry_spec(domain, spacing, origin, (nx, ny, nz), background_id)
+        pid = C.c_int32()
+        if tables is not None:
+            self._tables.append(tables)
+        N.check(N.load().midsx_server_add_phantom(self.handle, tables.handle if tables is not None else None,
+                                                  C.byref(spec), ids.ctypes.data, C.byref(pid)),
+                "midsx_server_add_phantom")
+        self._shapes[pid.value] = ids.shape
+        return pid.value
+
+    def submit(self, phantom, source, n, seed, first=0, precision="mixed", specs=(), dose_mode=N.DOSE_FULL):
+        arr = tally_specs(list(specs))
+        r = N.Request()
+        r.phantom = int(phantom)
+        r.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        r.dose_mode = int(dose_mode)
+        r.n_tallies = len(specs)
+        r.tallies = C.cast(arr, C.POINTER(N.TallySpec))
+        r.source = source.handle
+        r.seed, r.first_history, r.n_histories = int(seed), int(first), int(n)
+        rid = C.c_uint64()
+        N.check(N.load().midsx_server_submit(self.handle, C.byref(r), C.byref(rid)), "midsx_server_submit")
+        self._requests[rid.value] = (source, list(specs), int(dose_mode), int(phantom))
+        return rid.value
+
+    def poll(self, rid):
+        info = N.RequestInfo()
+        N.check(N.load().midsx_server_poll(self.handle, int(rid), C.byref(info)), "midsx_server_poll")
+        return info.as_dict()
+
+    def wait(self, rid, timeout=600.0):
+        info = N.RequestInfo()
+        N.check(N.load().midsx_server_wait(self.handle, int(rid), float(timeout), C.byref(info)),
+                "midsx_server_wait")
+        d = info.as_dict()
+        if d["state"] == N.REQ_FAILED:
+            raise N.MidsxError(d["status"], "request %d" % rid)
+        return d
+
+    def tallies(self, rid):
+        h = C.c_void_p()
+        N.check(N.load().midsx_server_tallies(self.handle, int(rid), C.byref(h)), "midsx_server_tallies")
+        _, specs, dose_mode, pid = self._requests[rid]
+        return TallyView(h, self._shapes[pid], specs, dose_mode)
+
+    def release(self, rid):
+        N.check(N.load().midsx_server_release(self.handle, int(rid)), "midsx_server_release")
+        self._requests.pop(rid, None)
+
+    def stats(self):
+        st = N.ServerStats()
+        N.check(N.load().midsx_server_get_stats(self.handle, C.byref(st)), "midsx_server_get_stats")
+        return st.as_dict()
+
+    def now(self):
+        t = C.c_double()
+        N.check(N.load().midsx_server_now(self.handle, C.byref(t)), "midsx_server_now")
+        return t.value
+
+    def close(self):
+        if self.handle:
+            N.load().midsx_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

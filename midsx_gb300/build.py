@@ -98,6 +98,7 @@ def build(verbose=False, with_oracle=True):
     nvcc = _nvcc()
     units = [
         ("transport.cu", [nvcc] + NVCC_FLAGS),
+        ("server.cu", [nvcc] + NVCC_FLAGS),
         ("tables.cpp", ["g++"] + CXX_FLAGS),
     ]
     core_units = [f for f in sorted(os.listdir(CSRC)) if f.startswith("core_") and f.endswith(".cpp")]

@@ -447,7 +447,8 @@ struct midsx_gpu_tallies {
     unsigned long long* acc = nullptr;  // all scalar/binned accumulators
     size_t acc_words = 0;
     unsigned long long* stats = nullptr;
-    int precision = -1;  // precision of the accumulated contents, -1 = empty
+    int precision = -1;   // precision of the accumulated contents, -1 = empty
+    bool pooled = false;  // one pool block starting at `stats`, owned by a request server
 };
 
 namespace {
@@ -845,17 +846,20 @@ extern "C" midsx_status midsx_gpu_source_destroy(midsx_source_h s) {
     return MIDSX_OK;
 }
 
-extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const midsx_tally_spec* specs,
-                                                 int32_t n_specs, int32_t dose_mode, midsx_tallies_h* out) {
-    if (!out || n_specs < 0 || n_specs > MIDSX_MAX_TALLIES || (n_specs > 0 && !specs) || dose_mode < 0 ||
-        dose_mode > 2 || (dose_mode > 0 && !phantom)) {
+namespace {
+
+// Validates the tally specs and lays out the handle on the host: device records with
+// accumulator offsets (relative to `acc`, fixed once it is allocated), accumulator and dose
+// sizes.  Allocates nothing on the device.
+midsx_status tallies_layout(size_t n_voxels, const midsx_tally_spec* specs, int32_t n_specs, int32_t dose_mode,
+                            midsx_gpu_tallies* t) {
+    if (n_specs < 0 || n_specs > MIDSX_MAX_TALLIES || (n_specs > 0 && !specs) || dose_mode < 0 || dose_mode > 2) {
         set_last_error("midsx_gpu_tallies_create: invalid argument");
         return MIDSX_INVALID_ARG;
     }
-    auto* t = new midsx_gpu_tallies();
     t->dose_mode = dose_mode;
     t->dose_stride = dose_mode == 0 ? 0 : (dose_mode == 1 ? 1 : 4);
-    t->n_voxels = phantom ? phantom->n_voxels : 0;
+    t->n_voxels = n_voxels;
     size_t words = 0;
     for (int i = 0; i < n_specs; ++i) {
         const midsx_tally_spec& s = specs[i];
@@ -875,7 +879,6 @@ extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const 
         } else if (s.kind == MIDSX_TALLY_SURFACE_RECT || s.kind == MIDSX_TALLY_SURFACE_BINNED_RECT) {
             double dd = s.b[0] * s.c[0] + s.b[1] * s.c[1] + s.b[2] * s.c[2];
             if (std::fabs(dd) >= 1e-9) {
-                delete t;
                 set_last_error("Edges are not orthogonal");
                 return MIDSX_INVALID_ARG;
             }
@@ -886,12 +889,10 @@ extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const 
             d.e1e1 = s.b[0] * s.b[0] + s.b[1] * s.b[1] + s.b[2] * s.b[2];
             d.e2e2 = s.c[0] * s.c[0] + s.c[1] * s.c[1] + s.c[2] * s.c[2];
             if (s.kind == MIDSX_TALLY_SURFACE_BINNED_RECT && (s.nu < 1 || s.nv < 1)) {
-                delete t;
                 set_last_error("binned tally needs nu, nv >= 1");
                 return MIDSX_INVALID_ARG;
             }
         } else if (s.kind != MIDSX_TALLY_VOLUME_AACUBOID) {
-            delete t;
             set_last_error("unknown tally kind");
             return MIDSX_INVALID_ARG;
         }
@@ -904,11 +905,36 @@ extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const 
         d.fradius = float(d.radius);
         d.fe1e1 = float(d.e1e1);
         d.fe2e2 = float(d.e2e2);
-        d.acc = reinterpret_cast<unsigned long long*>(words);  // offset, fixed below
+        d.acc = reinterpret_cast<unsigned long long*>(words);  // offset, fixed after allocation
         words += (s.kind == MIDSX_TALLY_SURFACE_BINNED_RECT) ? size_t(s.nu) * s.nv * 8 : kScalarWords;
         t->host_specs.push_back(d);
     }
     t->acc_words = words;
+    return MIDSX_OK;
+}
+
+// Device bytes of a laid-out handle: statistics (+ the launch counter word), accumulators,
+// tally records and the dose grid.
+size_t tallies_bytes(const midsx_gpu_tallies* t) {
+    return (kStCount + 1) * 8 + t->acc_words * 8 + t->host_specs.size() * sizeof(DevTally) +
+           t->n_voxels * size_t(t->dose_stride) * 8;
+}
+
+}  // namespace
+
+extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const midsx_tally_spec* specs,
+                                                 int32_t n_specs, int32_t dose_mode, midsx_tallies_h* out) {
+    if (!out || (dose_mode > 0 && !phantom)) {
+        set_last_error("midsx_gpu_tallies_create: invalid argument");
+        return MIDSX_INVALID_ARG;
+    }
+    auto* t = new midsx_gpu_tallies();
+    midsx_status lst = tallies_layout(phantom ? phantom->n_voxels : 0, specs, n_specs, dose_mode, t);
+    if (lst != MIDSX_OK) {
+        delete t;
+        return lst;
+    }
+    const size_t words = t->acc_words;
     // run statistics plus one word: the launch's history counter
     if (!cuda_ok(cudaMalloc(&t->stats, (kStCount + 1) * sizeof(unsigned long long)), "cudaMalloc") ||
         (words && !cuda_ok(cudaMalloc(&t->acc, words * 8), "cudaMalloc")) ||
@@ -930,6 +956,10 @@ extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const 
 
 extern "C" midsx_status midsx_gpu_tallies_destroy(midsx_tallies_h t) {
     if (!t) return MIDSX_INVALID_ARG;
+    if (t->pooled) {
+        set_last_error("these tallies belong to a request server: release the request instead");
+        return MIDSX_INVALID_ARG;
+    }
     cudaFree(t->dose);
     cudaFree(t->specs);
     cudaFree(t->acc);
@@ -949,6 +979,25 @@ extern "C" midsx_status midsx_gpu_tallies_reset(midsx_tallies_h t, void* stream)
 }
 
 namespace {
+
+// Checks that a job's handles belong together: phantom made with `tables`, dose tally sized
+// for the phantom, source energies inside the tables.
+midsx_status check_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_source_h source,
+                       midsx_tallies_h tallies, const std::string& what) {
+    if (!phantom || !source || !tallies || phantom->tables != tables) {
+        set_last_error(what + ": missing handle or phantom made with other tables");
+        return MIDSX_INVALID_ARG;
+    }
+    if (tallies->dose && tallies->n_voxels != phantom->n_voxels) {
+        set_last_error(what + ": dose tally size differs from the phantom");
+        return MIDSX_INVALID_ARG;
+    }
+    if (source->max_energy > tables->T.e_max) {
+        set_last_error(what + ": source energy above the tables' e_max");
+        return MIDSX_TABLE_RANGE;
+    }
+    return MIDSX_OK;
+}
 
 void fill_job(DevJob& J, midsx_phantom_h phantom, midsx_source_h source, midsx_tallies_h tallies, uint64_t seed,
               uint64_t first, uint64_t n) {
@@ -1414,20 +1463,10 @@ extern "C" midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const mids
     b->host_prefix.push_back(0);
     for (int i = 0; i < n_jobs; ++i) {
         const midsx_batch_job& j = jobs[i];
-        if (!j.phantom || !j.source || !j.tallies || j.phantom->tables != tables) {
+        midsx_status cst = check_job(tables, j.phantom, j.source, j.tallies, "batch job " + std::to_string(i));
+        if (cst != MIDSX_OK) {
             delete b;
-            set_last_error("batch job " + std::to_string(i) + ": missing handle or phantom made with other tables");
-            return MIDSX_INVALID_ARG;
-        }
-        if (j.tallies->dose && j.tallies->n_voxels != j.phantom->n_voxels) {
-            delete b;
-            set_last_error("batch job " + std::to_string(i) + ": dose tally size differs from the phantom");
-            return MIDSX_INVALID_ARG;
-        }
-        if (j.source->max_energy > tables->T.e_max) {
-            delete b;
-            set_last_error("batch job " + std::to_string(i) + ": source energy above the tables' e_max");
-            return MIDSX_TABLE_RANGE;
+            return cst;
         }
         DevJob d;
         std::memset(&d, 0, sizeof(d));
@@ -1598,3 +1637,149 @@ extern "C" midsx_status midsx_gpu_stream_destroy(void* stream) {
 }
 
 extern "C" midsx_status midsx_gpu_stream_synchronize(void* stream) { return wait_stream(stream); }
+
+// ============================================== internal runtime for the request server ===
+#include "runtime.h"
+
+namespace midsx {
+namespace rt {
+
+size_t job_record_bytes() { return sizeof(DevJob); }
+
+midsx_status pack_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_source_h source,
+                      midsx_tallies_h tallies, uint64_t seed, uint64_t first, uint64_t n, int precision,
+                      void* dst) {
+    if (!tables || !phantom || !source || !tallies || !dst) return MIDSX_INVALID_ARG;
+    midsx_status st = check_job(tables, phantom, source, tallies, "job");
+    if (st != MIDSX_OK) return st;
+    if (precision != MIDSX_PREC_FP64 && precision != MIDSX_PREC_MIXED) {
+        set_last_error("unknown precision");
+        return MIDSX_INVALID_ARG;
+    }
+    if (precision == MIDSX_PREC_MIXED && source->max_energy > kMixedMaxEnergy) {
+        set_last_error("the mixed form's fixed-point tallies take source energies up to 262144 eV");
+        return MIDSX_INVALID_ARG;
+    }
+    if (tallies->precision >= 0 && tallies->precision != precision) {
+        set_last_error("tallies hold results of the other precision");
+        return MIDSX_INVALID_ARG;
+    }
+    if (!phantom->ids) {
+        set_last_error("phantom not resident on the device");
+        return MIDSX_INVALID_ARG;
+    }
+    DevJob d;
+    std::memset(&d, 0, sizeof(d));
+    fill_job(d, phantom, source, tallies, seed, first, n);
+    std::memcpy(dst, &d, sizeof(d));
+    return MIDSX_OK;
+}
+
+midsx_status launch_packed(midsx_tables_h tables, const void* dev_jobs, int n_jobs,
+                           const unsigned long long* dev_prefix, unsigned long long total,
+                           unsigned long long* dev_counter, const midsx_run_config& cfg, cudaStream_t s) {
+    if (!tables || !dev_jobs || !dev_prefix || !dev_counter || n_jobs < 1 || n_jobs > kMaxBatchJobs)
+        return MIDSX_INVALID_ARG;
+    if (cfg.precision != MIDSX_PREC_FP64 && cfg.precision != MIDSX_PREC_MIXED) {
+        set_last_error("unknown precision");
+        return MIDSX_INVALID_ARG;
+    }
+    if (total == 0) return MIDSX_OK;
+    RunParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.T = tables->T;
+    P.jobs = static_cast<const DevJob*>(dev_jobs);
+    P.n_jobs = n_jobs;
+    P.prefix = dev_prefix;
+    P.counter = dev_counter;
+    P.total = total;
+    return launch_kernel(tables, P, cfg, true, s);
+}
+
+size_t tallies_footprint(size_t n_voxels, const midsx_tally_spec* specs, int n_specs, int dose_mode) {
+    midsx_gpu_tallies t;
+    if (tallies_layout(n_voxels, specs, n_specs, dose_mode, &t) != MIDSX_OK) return 0;
+    return tallies_bytes(&t);
+}
+
+midsx_status tallies_create_async(midsx_phantom_h phantom, const midsx_tally_spec* specs, int n_specs,
+                                  int dose_mode, cudaMemPool_t pool, cudaStream_t s, midsx_tallies_h* out) {
+    if (!out || !pool || (dose_mode > 0 && !phantom)) return MIDSX_INVALID_ARG;
+    auto* t = new midsx_gpu_tallies();
+    midsx_status st = tallies_layout(phantom ? phantom->n_voxels : 0, specs, n_specs, dose_mode, t);
+    if (st != MIDSX_OK) {
+        delete t;
+        return st;
+    }
+    // one allocation: statistics, accumulators, tally records, dose grid (8-byte words each)
+    const size_t bytes = tallies_bytes(t);
+    unsigned char* base = nullptr;
+    cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&base), bytes, pool, s);
+    if (e != cudaSuccess) {
+        delete t;
+        cuda_ok(e, "cudaMallocFromPoolAsync");
+        return e == cudaErrorMemoryAllocation ? MIDSX_OOM : MIDSX_CUDA_ERROR;
+    }
+    size_t off = 0;
+    t->stats = reinterpret_cast<unsigned long long*>(base + off);
+    off += (kStCount + 1) * 8;
+    if (t->acc_words) t->acc = reinterpret_cast<unsigned long long*>(base + off);
+    off += t->acc_words * 8;
+    if (!t->host_specs.empty()) t->specs = reinterpret_cast<DevTally*>(base + off);
+    off += t->host_specs.size() * sizeof(DevTally);
+    if (t->dose_stride) t->dose = reinterpret_cast<unsigned long long*>(base + off);
+    for (auto& d : t->host_specs) d.acc = t->acc + reinterpret_cast<size_t>(d.acc);
+    bool ok = cuda_ok(cudaMemsetAsync(base, 0, bytes, s), "cudaMemsetAsync");
+    // the records are copied from the handle's own host vector, which outlives the copy
+    if (ok && !t->host_specs.empty())
+        ok = cuda_ok(cudaMemcpyAsync(t->specs, t->host_specs.data(), t->host_specs.size() * sizeof(DevTally),
+                                     cudaMemcpyHostToDevice, s),
+                     "cudaMemcpyAsync");
+    if (!ok) {
+        cudaFreeAsync(base, s);
+        delete t;
+        return MIDSX_CUDA_ERROR;
+    }
+    t->pooled = true;
+    *out = t;
+    return MIDSX_OK;
+}
+
+void tallies_destroy_async(midsx_tallies_h t, cudaStream_t s) {
+    if (!t) return;
+    if (t->pooled)
+        cudaFreeAsync(t->stats, s);  // the block starts at the statistics
+    delete t;
+}
+
+void set_tallies_precision(midsx_tallies_h t, int precision) {
+    if (t) t->precision = precision;
+}
+
+size_t phantom_voxels(midsx_phantom_h p) { return p ? p->n_voxels : 0; }
+
+midsx_status phantom_download(midsx_phantom_h p, std::vector<uint8_t>& dense) {
+    if (!p || !p->ids) return MIDSX_INVALID_ARG;
+    dense.resize(p->n_voxels);
+    CUDA_TRY(cudaMemcpy(dense.data(), p->ids, p->n_voxels, cudaMemcpyDeviceToHost));
+    return MIDSX_OK;
+}
+
+uint8_t* phantom_storage(midsx_phantom_h p) { return p ? p->ids : nullptr; }
+
+void phantom_bind(midsx_phantom_h p, uint8_t* dense_ids) {
+    p->ids = dense_ids;
+    p->G.ids = dense_ids;
+}
+
+void phantom_drop_storage(midsx_phantom_h p) {
+    if (p && p->ids) cudaFree(p->ids);
+    phantom_bind(p, nullptr);
+}
+
+void phantom_delete_handle(midsx_phantom_h p) { delete p; }
+
+int tables_device(midsx_tables_h t) { return t ? t->device : 0; }
+
+}  // namespace rt
+}  // namespace midsx

@@ -101,6 +101,41 @@ VP = C.c_void_p
 PD = C.POINTER(C.c_double)
 PI64 = C.POINTER(C.c_int64)
 
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("launch_histories", C.c_uint64),
+                ("max_active", C.c_int32), ("launches_in_flight", C.c_int32), ("launch", RunConfig)]
+
+
+class Request(C.Structure):
+    _fields_ = [("phantom", C.c_int32), ("precision", C.c_int32), ("dose_mode", C.c_int32),
+                ("n_tallies", C.c_int32), ("tallies", C.POINTER(TallySpec)), ("source", VP),
+                ("seed", C.c_uint64), ("first_history", C.c_uint64), ("n_histories", C.c_uint64)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("launches", C.c_int32), ("reserved", C.c_int32),
+                ("histories_scheduled", C.c_uint64), ("histories_done", C.c_uint64),
+                ("footprint_bytes", C.c_uint64), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_first_launch", C.c_double), ("t_done", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "submitted", "admitted", "completed", "failed", "launches", "histories", "budget_bytes",
+        "bytes_in_use", "peak_bytes_in_use", "resident_phantom_bytes", "phantom_uploads",
+        "phantom_evictions")] + [(n, C.c_int32) for n in ("queued", "active", "max_active_seen", "reserved")] + [
+        ("busy_seconds", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 _SIGNATURES = {
     "midsx_tables_build": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.c_int32, C.c_double,
                                      C.POINTER(C.POINTER(TableBlob))]),
@@ -141,6 +176,16 @@ _SIGNATURES = {
     "midsx_gpu_batch_autotune": (C.c_int, [VP, C.c_int32, C.c_uint64, C.POINTER(RunConfig), PD, VP]),
     "midsx_gpu_trace_deposits": (C.c_int, [VP, VP, VP, C.POINTER(RunConfig), PD]),
     "midsx_gpu_trace_deposits_noalloc": (C.c_int, [VP, VP, VP, C.POINTER(RunConfig), PD, VP]),
+    "midsx_server_create": (C.c_int, [VP, C.POINTER(ServerConfig), C.POINTER(VP)]),
+    "midsx_server_destroy": (C.c_int, [VP]),
+    "midsx_server_add_phantom": (C.c_int, [VP, VP, C.POINTER(GeometrySpec), C.c_void_p, C.POINTER(C.c_int32)]),
+    "midsx_server_submit": (C.c_int, [VP, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    "midsx_server_poll": (C.c_int, [VP, C.c_uint64, C.POINTER(RequestInfo)]),
+    "midsx_server_wait": (C.c_int, [VP, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]),
+    "midsx_server_tallies": (C.c_int, [VP, C.c_uint64, C.POINTER(VP)]),
+    "midsx_server_release": (C.c_int, [VP, C.c_uint64]),
+    "midsx_server_get_stats": (C.c_int, [VP, C.POINTER(ServerStats)]),
+    "midsx_server_now": (C.c_int, [VP, PD]),
 }
 
 _lib = None

@@ -165,9 +165,12 @@ def batch_jobs(n_jobs=64, seed=1, edge_range=(32, 256), kvp_range=(20.0, 120.0),
 
 
 def radiography(n_histories=1_000_000_000, shape=(256, 512, 512), spacing=0.05, seed=1, det_bins=512,
-                det_pitch=0.1, sid=100.0, kvp=100.0):
+                det_pitch=0.1, sid=100.0, kvp=100.0, lead_spheres=16):
+    """Projection radiograph: phantom midway between a point source and a det_bins^2
+    detector of det_pitch cm bins at `sid` cm (primary and scattered fluence per bin).  With
+    lead_spheres=0 the tables hold the four tissue materials only (no lead majorant)."""
     nz, ny, nx = shape
-    ids = ellipsoid_phantom(shape, spacing, seed, lead_spheres=16)
+    ids = ellipsoid_phantom(shape, spacing, seed, lead_spheres=lead_spheres)
     ext = np.array([nx, ny, nz]) * spacing
     det = det_bins * det_pitch
     width = max(det, ext[0])
@@ -178,6 +181,71 @@ def radiography(n_histories=1_000_000_000, shape=(256, 512, 512), spacing=0.05, 
     specs = [dict(kind="binned", corner=corner, edge1=(det, 0, 0), edge2=(0, det, 0), nu=det_bins, nv=det_bins)]
     source = dict(position=src_pos, direction=("disc", (width / 2, width / 2, sid), (0, 0, 1), det / 2),
                   spectrum=kramers_spectrum(kvp))
-    return Scene("radiography_%dx%dx%d_%gkVp" % (nx, ny, nz, kvp),
-                 [AIR, SOFT_TISSUE, ADIPOSE, CORTICAL_BONE, LEAD], domain, (spacing,) * 3, origin, ids, AIR,
-                 source, specs, DOSE_SUM, n_histories, 150e3)
+    materials = [AIR, SOFT_TISSUE, ADIPOSE, CORTICAL_BONE] + ([LEAD] if lead_spheres else [])
+    return Scene("radiography_%dx%dx%d_%gkVp" % (nx, ny, nz, kvp), materials, domain, (spacing,) * 3, origin, ids,
+                 AIR, source, specs, DOSE_SUM, n_histories, 150e3)
+
+
+def dose_job(edge, spacing=0.1, seed=1, kvp=80.0, n_histories=1_000_000, al=None):
+    """A dose request: edge^3 seeded ellipsoid phantom at `spacing` cm, Kramers spectrum at
+    kvp, disc-collimated point source 10 cm in front of the phantom, per-voxel dose tally."""
+    shape = (edge, edge, edge)
+    ids = ellipsoid_phantom(shape, spacing, seed=seed, n_ellipsoids=max(4, edge // 8))
+    ext = edge * spacing
+    z0 = 10.5
+    spectrum = kramers_spectrum(kvp, e_min=min(10.0, kvp - 5.0), tables=al)
+    source = dict(position=(ext / 2, ext / 2, 0.5), direction=("disc", (ext / 2, ext / 2, z0), (0, 0, 1), ext / 2),
+                  spectrum=spectrum)
+    return Scene("dose_%d^3_%gkVp" % (edge, kvp), [AIR, SOFT_TISSUE, ADIPOSE, CORTICAL_BONE],
+                 (ext, ext, z0 + ext + 1.0), (spacing,) * 3, (0.0, 0.0, z0), ids, AIR, source, [], DOSE_FULL,
+                 n_histories, 150e3)
+
+
+SERVING_CLASSES = (
+    # name, probability, histories
+    ("small_dose_64^3", 0.70, 1_000_000),
+    ("medium_dose_128^3", 0.25, 10_000_000),
+    ("radiography_256x256x128", 0.05, 100_000_000),
+)
+
+
+def serving_templates(pool=4, seed=1, small_edge=64, medium_edge=128, radio_shape=(128, 256, 256), radio_bins=256,
+                      radio_lead=0):
+    """Phantom/source/tally templates of the serving mix: `pool` seeded phantoms per class.
+    Dose classes: small_edge^3 and medium_edge^3 at 1 mm with a full dose tally; radiography:
+    radio_shape at 0.5 mm (radio_lead lead spheres) with a radio_bins^2 detector of 2 mm bins
+    at 100 cm SID and no dose tally.  Returns {class name: [Scene]}."""
+    al = api.TableBlob([ALUMINIUM], e_max=150e3)
+    kvps = (60.0, 80.0, 100.0, 120.0)
+    out = {}
+    for ci, (name, _, n) in enumerate(SERVING_CLASSES):
+        scenes = []
+        for k in range(pool):
+            s = seed * 1000 + ci * 100 + k
+            if ci < 2:
+                edge = small_edge if ci == 0 else medium_edge
+                scenes.append(dose_job(edge, 0.1, s, kvps[k % len(kvps)], n, al))
+            else:
+                sc = radiography(n, shape=radio_shape, spacing=0.05, seed=s, det_bins=radio_bins,
+                                 det_pitch=0.2, kvp=100.0, lead_spheres=radio_lead)
+                sc.dose_mode = 0
+                scenes.append(sc)
+        out[name] = scenes
+    return out
+
+
+def serving_requests(rate=200.0, n_requests=400, seed=1, pool=4, hist_scale=1.0):
+    """A seeded Poisson stream of requests over the classes of SERVING_CLASSES: arrival time
+    (s), class name, template index, history count (times hist_scale), seed and first id."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n_requests))
+    names = [c[0] for c in SERVING_CLASSES]
+    probs = np.array([c[1] for c in SERVING_CLASSES])
+    cls = rng.choice(len(names), size=n_requests, p=probs / probs.sum())
+    tmpl = rng.integers(0, pool, size=n_requests)
+    out = []
+    for i in range(n_requests):
+        n = max(1, int(SERVING_CLASSES[cls[i]][2] * hist_scale))
+        out.append(dict(t=float(t[i]), cls=names[cls[i]], template=int(tmpl[i]), n=n, seed=seed * 100000 + i,
+                        first=0))
+    return out

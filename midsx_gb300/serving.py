@@ -1,0 +1,136 @@
+"""Load driver for the request server: registers the serving mix's phantoms, submits a
+seeded Poisson stream of requests at their arrival times from one thread, and retires them
+from another (reads each result to host memory, then releases it).  Reports throughput and
+request latencies.
+
+Latency of a request = time from its arrival (submission) to the moment its results are in
+host memory; the server-side part (submission to the end of its last launch) is reported
+beside it.
+"""
+import threading
+import time
+
+import numpy as np
+
+from . import api
+from . import native as N
+from . import scenes
+
+
+class Mix:
+    """The serving mix on one server: tables per material set (the dose classes carry no lead,
+    the radiography class does, so dose requests keep a soft-tissue majorant), registered
+    phantoms and one source per template."""
+
+    def __init__(self, templates, server_kw=None):
+        self.templates = templates
+        self.tables = {}
+        for scs in templates.values():
+            for sc in scs:
+                key = tuple(sc.materials)
+                if key not in self.tables:
+                    self.tables[key] = api.Tables(list(key), e_max=max(s.e_max for v in templates.values()
+                                                                       for s in v))
+        default = self.tables[tuple(templates[scenes.SERVING_CLASSES[0][0]][0].materials)]
+        self.server = api.Server(default, **(server_kw or {}))
+        self.pid = {}
+        self.source = {}
+        for name, scs in templates.items():
+            for k, sc in enumerate(scs):
+                t = self.tables[tuple(sc.materials)]
+                self.pid[name, k] = self.server.add_phantom(sc.domain, sc.spacing, sc.origin, sc.ids, sc.background,
+                                                            tables=None if t is default else t)
+                self.source[name, k] = api.Source(**sc.source)
+
+    def submit(self, req, precision="mixed"):
+        sc = self.templates[req["cls"]][req["template"]]
+        key = (req["cls"], req["template"])
+        return self.server.submit(self.pid[key], self.source[key], req["n"], req["seed"], req.get("first", 0),
+                                  precision, sc.specs, sc.dose_mode)
+
+    def read(self, rid, req):
+        """Results of a done request in host memory (dose arrays or detector images)."""
+        sc = self.templates[req["cls"]][req["template"]]
+        tl = self.server.tallies(rid)
+        out = {"stats": tl.stats()}
+        if sc.dose_mode:
+            out["dose"] = tl.dose()
+        for i, spec in enumerate(sc.specs):
+            if spec["kind"] == "binned":
+                out["binned%d" % i] = tl.binned(i)
+        return out
+
+    def close(self):
+        self.server.close()
+
+
+def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3600.0):
+    """Plays `requests` (scenes.serving_requests) against mix.server in real time.  Returns a
+    dict of per-request records and summary figures; keep=True also returns the results."""
+    n = len(requests)
+    rids = [None] * n
+    t_arr = [None] * n
+    t_host = [None] * n
+    infos = [None] * n
+    results = [None] * n if keep else None
+    errors = []
+    submitted = threading.Semaphore(0)
+
+    def retire():
+        pending = []  # indices of submitted, not yet retired requests
+        next_idx = 0
+        got = 0
+        deadline = time.perf_counter() + timeout
+        while got < n and time.perf_counter() < deadline:
+            while submitted.acquire(blocking=False):
+                pending.append(next_idx)
+                next_idx += 1
+            progressed = False
+            for i in list(pending):
+                info = mix.server.poll(rids[i])
+                if info["state"] in (N.REQ_DONE, N.REQ_FAILED):
+                    if info["state"] == N.REQ_DONE:
+                        res = mix.read(rids[i], requests[i])
+                        if keep:
+                            results[i] = res
+                    else:
+                        errors.append((i, info["status"]))
+                    t_host[i] = time.perf_counter()
+                    infos[i] = info
+                    mix.server.release(rids[i])
+                    pending.remove(i)
+                    got += 1
+                    progressed = True
+            if not progressed:
+                time.sleep(poll_s)
+
+    th = threading.Thread(target=retire)
+    th.start()
+    t0 = time.perf_counter()
+    for i, req in enumerate(requests):
+        delay = t0 + req["t"] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        t_arr[i] = time.perf_counter()
+        rids[i] = mix.submit(req, precision)
+        submitted.release()
+    th.join()
+    t_end = max(t for t in t_host if t is not None)
+    lat = np.array([t_host[i] - t_arr[i] for i in range(n) if t_host[i] is not None])
+    srv = np.array([infos[i]["t_done"] - infos[i]["t_submit"] for i in range(n) if infos[i] is not None])
+    hist = sum(r["n"] for r in requests)
+    span = t_end - t0
+    by_cls = {}
+    for c in sorted({r["cls"] for r in requests}):
+        li = [t_host[i] - t_arr[i] for i in range(n) if requests[i]["cls"] == c and t_host[i] is not None]
+        by_cls[c] = {"requests": len(li), "p50_ms": 1e3 * float(np.median(li)) if li else None,
+                     "p99_ms": 1e3 * float(np.percentile(li, 99)) if li else None}
+    out = {"requests": n, "failed": len(errors), "histories": hist, "span_s": span,
+           "histories_per_s": hist / span, "offered_histories_per_s": hist / max(requests[-1]["t"], 1e-9),
+           "latency_ms": {"p50": 1e3 * float(np.median(lat)), "p99": 1e3 * float(np.percentile(lat, 99)),
+                          "max": 1e3 * float(lat.max())},
+           "server_latency_ms": {"p50": 1e3 * float(np.median(srv)), "p99": 1e3 * float(np.percentile(srv, 99))},
+           "by_class": by_cls, "server": mix.server.stats()}
+    if keep:
+        out["results"] = results
+    return out

@@ -256,3 +256,28 @@ def test_scenes_are_deterministic():
     np.testing.assert_array_equal(a, b)
     e, w = scenes.kramers_spectrum(80.0)
     assert e.size == 71 and w[-1] == 0 and np.all(w[:-1] > 0)
+
+
+def test_serving_stream_is_seeded_poisson_with_the_class_mix():
+    a = scenes.serving_requests(rate=200.0, n_requests=4000, seed=1)
+    b = scenes.serving_requests(rate=200.0, n_requests=4000, seed=1)
+    assert a == b
+    t = np.array([r["t"] for r in a])
+    gaps = np.diff(np.concatenate([[0.0], t]))
+    assert np.all(gaps > 0) and abs(gaps.mean() - 1 / 200.0) < 0.1 / 200.0
+    frac = {c: np.mean([r["cls"] == c for r in a]) for c, _, _ in scenes.SERVING_CLASSES}
+    for c, p, n in scenes.SERVING_CLASSES:
+        assert abs(frac[c] - p) < 0.03, (c, frac[c])
+        assert all(r["n"] == n for r in a if r["cls"] == c)
+    assert len({r["seed"] for r in a}) == len(a)
+
+
+def test_serving_templates_shapes_and_tables():
+    tm = scenes.serving_templates(pool=2, seed=3, small_edge=16, medium_edge=24, radio_shape=(16, 32, 32),
+                                  radio_bins=32)
+    assert [sc.ids.shape for sc in tm["small_dose_64^3"]] == [(16, 16, 16)] * 2
+    radio = tm["radiography_256x256x128"][0]
+    assert radio.dose_mode == 0 and radio.specs[0]["nu"] == 32 and scenes.LEAD not in radio.materials
+    lead = scenes.serving_templates(pool=1, seed=3, small_edge=8, medium_edge=8, radio_shape=(16, 32, 32),
+                                    radio_bins=8, radio_lead=2)["radiography_256x256x128"][0]
+    assert scenes.LEAD in lead.materials and (lead.ids == scenes.LEAD).any()
