@@ -163,7 +163,42 @@ MIDSX_HD float fabs_(float v) { return fabsf(v); }
 // to v built from its smallest component, then by phi about v, as the quaternion product
 // q = q_phi * q_theta applied as q v q^-1 (particle.cpp:7-45).
 template <typename R>
+MIDSX_HD V3<R> rotate_half(const V3<R>& v, R st, R ct, R sp, R cp);
+
+template <typename R>
 MIDSX_HD V3<R> rotate_direction(const V3<R>& v, R theta, R phi) {
+    R st, ct, sp, cp;
+    sincos_(theta / R(2), &st, &ct);
+    sincos_(phi / R(2), &sp, &cp);
+    return rotate_half(v, st, ct, sp, cp);
+}
+
+// New direction at polar cosine mu and azimuth 2 pi u: rotateDirection with theta = acos mu
+// and phi = 2 pi u.  The FP64 form evaluates acos and the half-angle sincos as the reference
+// does; the FP32 form takes the half angles from mu and u directly - cos(theta/2) =
+// sqrt((1 + mu) / 2), sin(theta/2) = sqrt((1 - mu) / 2), (sin, cos)(phi/2) = sincospi(u) -
+// with no acos and no trigonometric range reduction.  A mu outside [-1, 1] gives a NaN
+// direction in both forms.
+template <typename R>
+MIDSX_HD V3<R> scatter_direction(const V3<R>& v, R mu, R u) {
+    if constexpr (sizeof(R) == 8) {
+        return rotate_direction(v, acos_(mu), R(2 * kPi) * u);
+    } else {
+        const R st = sqrt_((R(1) - mu) * R(0.5)), ct = sqrt_((R(1) + mu) * R(0.5));
+        R sp, cp;
+#if defined(__CUDA_ARCH__)
+        sincospif(u, &sp, &cp);
+#else
+        sp = std::sin(R(kPi) * u);
+        cp = std::cos(R(kPi) * u);
+#endif
+        return rotate_half(v, st, ct, sp, cp);
+    }
+}
+
+// rotateDirection from the half-angle sines and cosines of theta and phi.
+template <typename R>
+MIDSX_HD V3<R> rotate_half(const V3<R>& v, R st, R ct, R sp, R cp) {
     V3<R> p;
     R ax = fabs_(v.x), ay = fabs_(v.y), az = fabs_(v.z);
     if (ax <= ay && ax <= az) {
@@ -179,9 +214,6 @@ MIDSX_HD V3<R> rotate_direction(const V3<R>& v, R theta, R phi) {
         p.y /= pn;
         p.z /= pn;
     }
-    R st, ct, sp, cp;
-    sincos_(theta / R(2), &st, &ct);
-    sincos_(phi / R(2), &sp, &cp);
     // q_theta = (ct, p st), q_phi = (cp, v sp)
     R tw = ct, tx = p.x * st, ty = p.y * st, tz = p.z * st;
     R fw = cp, fx = v.x * sp, fy = v.y * sp, fz = v.z * sp;
@@ -303,6 +335,59 @@ MIDSX_HD R spline_lookup(const DevTables& t, const DevSpline& S, R e) {
         hi = S.f_lx_max;
     }
     return spline_eval_at(D + S.knot_u, D + S.ctrl, S.degree, span, lo, hi, e);
+}
+
+// An energy query shared by several energy tables: the energy, its log10 and its bucket
+// (every energy table uses the same slice parametrisation), computed once.
+template <typename R>
+struct EnergyKey {
+    R q, lq;
+    int b;
+};
+
+template <typename R>
+MIDSX_HD EnergyKey<R> energy_key(const DevTables& t, R q) {
+    return {q, log10_(q), bucket_of(q, bspec<R>(t, 0))};
+}
+
+// lin_lookup of an energy table (kind 0) with a precomputed key: same index, same value.
+template <typename R>
+MIDSX_HD R lin_lookup_key(const DevTables& t, const DevLin& L, const EnergyKey<R>& k) {
+    const R* D = tab<R>(t);
+    const R* x = D + L.x;
+    int idx;
+    if (k.q <= x[0]) {
+        idx = 0;
+    } else if (k.q >= x[L.n - 1]) {
+        idx = L.n;
+    } else {
+        const int* st = buckets<R>(t, L.bk_d, L.bk_f);
+        idx = upper_index(x, st[k.b], st[k.b + 1], k.q);
+    }
+    return lin_eval_at_log(D + L.lx, D + L.ly, L.n, idx, k.lq);
+}
+
+// spline_lookup with a precomputed key: same span, same value.
+template <typename R>
+MIDSX_HD R spline_lookup_key(const DevTables& t, const DevSpline& S, const EnergyKey<R>& k) {
+    const R* D = tab<R>(t);
+    const R* ke = D + S.knot_e;
+    int span;
+    if (k.q <= ke[0]) {
+        span = S.degree;
+    } else {
+        const int* st = buckets<R>(t, S.bk_d, S.bk_f);
+        span = upper_index(ke, st[k.b], st[k.b + 1], k.q) - 1;
+    }
+    R lo, hi;
+    if constexpr (sizeof(R) == 8) {
+        lo = S.lx_min;
+        hi = S.lx_max;
+    } else {
+        lo = S.f_lx_min;
+        hi = S.f_lx_max;
+    }
+    return spline_eval_at_log(D + S.knot_u, D + S.ctrl, S.degree, span, lo, hi, k.lq);
 }
 
 // Lower RITA energy row (lower_bound - 1) with the bucketed search.

@@ -22,13 +22,31 @@
 // threshold (isDeltaScatter: p_delta = 1 - mu / mu_max), kept per thread in shared memory
 template <typename R>
 __device__ __noinline__ R refresh_energy(const RunParams& P, R E, R* thr, R* mu, int stride) {
-    R mu_max = lin_lookup<R>(P.T, P.T.majorant, E);
+    const EnergyKey<R> key = energy_key<R>(P.T, E);  // one log10 and bucket for every table
+    R mu_max = lin_lookup_key<R>(P.T, P.T.majorant, key);
     for (int m = 0; m < P.T.n_materials; ++m) {
-        R mm = lin_lookup<R>(P.T, P.T.mat[m].total, E);
+        R mm = lin_lookup_key<R>(P.T, P.T.mat[m].total, key);
         mu[m * stride] = mm;
         thr[m * stride] = R(1) - mm / mu_max;
     }
     return mu_max;
+}
+
+// setInteractionType's probabilities (physics_engine.cpp:82-109): coherent and incoherent
+// cross sections (LogLogSpline) over the material's total, at one energy key.  (Inlined: an
+// out-of-line copy measured 4-5 % slower, the call saving registers around it.)
+template <typename R>
+__device__ __forceinline__ void interaction_probs(const DevTables& T, const DevMaterial& Mt, R E, R mu_tot, R& p_coh,
+                                               R& p_incoh) {
+    const EnergyKey<R> key = energy_key<R>(T, E);
+    p_coh = spline_lookup_key<R>(T, Mt.coh, key) / mu_tot;
+    p_incoh = spline_lookup_key<R>(T, Mt.incoh, key) / mu_tot;
+}
+
+// scatter_direction for the coherent and incoherent branches.
+template <typename R>
+__device__ __forceinline__ V3<R> scatter_dir(const V3<R>& v, R mu, R u) {
+    return scatter_direction(v, mu, u);
 }
 
 // Compton scattering by Kahn's method with the S(x) rejection
@@ -121,7 +139,7 @@ __host__ __device__ inline size_t kernel_smem(int n_jobs, bool multi, int n_mate
 }
 
 template <typename R, bool MULTI>
-__global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(const RunParams P) {
     constexpr bool MX = sizeof(R) == 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int njobs = MULTI ? P.n_jobs : 1;
@@ -183,8 +201,10 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                 ++steps;
                 uint64_t w1, w2;
                 rng.next_pair64(w1, w2);
+                // getFreePath.  The FP32 form uses the hardware log2 (absolute error ~1e-7 near
+                // U = 1, clamped at zero so that a step never goes backwards).
                 if constexpr (MX)
-                    s = -log_(to_uniform(w1, R(0))) * inv_mu_max;
+                    s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) * inv_mu_max;
                 else
                     s = -log_(to_uniform(w1, R(0))) / mu_max;
                 p0 = pos;
@@ -300,8 +320,8 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                 // setInteractionType (physics_engine.cpp:82-109)
                 const DevMaterial& Mt = P.T.mat[mat];
                 const R mu_tot = mucache[mat * stride];
-                const R p_coh = spline_lookup<R>(P.T, Mt.coh, E) / mu_tot;
-                const R p_incoh = spline_lookup<R>(P.T, Mt.incoh, E) / mu_tot;
+                R p_coh, p_incoh;
+                interaction_probs<R>(P.T, Mt, E, mu_tot, p_coh, p_incoh);
                 const R u3 = uniform<R>(rng);
                 const int cls0 = scatter_class(n_coh, n_incoh);
                 const R E0 = E;
@@ -317,9 +337,7 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                         stat_add(st, kStRangeErr, 1);
                         failed = true;
                     } else {
-                        R theta = acos_(mu);
-                        R phi = R(2 * kPi) * uniform<R>(rng);
-                        dir = rotate_direction(dir, theta, phi);
+                        dir = scatter_dir(dir, mu, uniform<R>(rng));
                     }
                 } else if (u3 < p_coh + p_incoh) {
                     // IncoherentScattering::interact
@@ -331,9 +349,7 @@ __global__ void __launch_bounds__(256, 3) transport_kernel(const RunParams P) {
                         failed = true;
                     } else {
                         const R k = E / R(kMec2);
-                        R theta = acos_(mu);
-                        R phi = R(2 * kPi) * uniform<R>(rng);
-                        dir = rotate_direction(dir, theta, phi);
+                        dir = scatter_dir(dir, mu, uniform<R>(rng));
                         E = kp * R(kMec2);
                         dep = R(kMec2) * (k - kp);
                         energy_changed = true;

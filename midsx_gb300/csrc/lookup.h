@@ -97,7 +97,11 @@ MIDSX_HD int bucket_of(R q, const BucketSpec& s) {
 }
 
 MIDSX_HD double exp10_(double y) { return pow(10.0, y); }
+#if defined(__CUDA_ARCH__)
+MIDSX_HD float exp10_(float y) { return exp10f(y); }
+#else
 MIDSX_HD float exp10_(float y) { return powf(10.0f, y); }
+#endif
 MIDSX_HD double log10_(double y) { return log10(y); }
 MIDSX_HD float log10_(float y) { return log10f(y); }
 MIDSX_HD double log_(double y) { return log(y); }
@@ -116,15 +120,22 @@ MIDSX_HD int lin_index(const R* x, int n, R q) {
     return upper_index(x, 0, n, q);
 }
 
+// LogLogLinear value on interval idx, given lq = log10(q).  Tables queried at one energy
+// share the logarithm.
 template <typename R>
-MIDSX_HD R lin_eval_at(const R* lx, const R* ly, int n, int idx, R q) {
+MIDSX_HD R lin_eval_at_log(const R* lx, const R* ly, int n, int idx, R lq) {
     if (idx == 0) return exp10_(ly[0]);
     if (idx >= n) return exp10_(ly[n - 1]);
-    R lq = log10_(q);
     R x1 = lx[idx - 1], x2 = lx[idx];
     R y1 = ly[idx - 1], y2 = ly[idx];
     R slope = (y2 - y1) / (x2 - x1);
     return exp10_(y1 + slope * (lq - x1));
+}
+
+template <typename R>
+MIDSX_HD R lin_eval_at(const R* lx, const R* ly, int n, int idx, R q) {
+    if (idx == 0 || idx >= n) return lin_eval_at_log(lx, ly, n, idx, R(0));
+    return lin_eval_at_log(lx, ly, n, idx, log10_(q));
 }
 
 template <typename R>
@@ -141,10 +152,11 @@ MIDSX_HD int spline_span(const R* knot_e, int n_ctrl, int degree, R e) {
     return upper_index(knot_e, degree - 1, n_knots - degree - 1, e) - 1;
 }
 
+// B-spline value at parameter u = (log10 e - lx_min) / (lx_max - lx_min), given le = log10 e.
 template <typename R>
-MIDSX_HD R spline_eval_at(const R* knot_u, const R* ctrl, int degree, int span, R lx_min,
-                          R lx_max, R e) {
-    R u = (log10_(e) - lx_min) / (lx_max - lx_min);
+MIDSX_HD R spline_eval_at_log(const R* knot_u, const R* ctrl, int degree, int span, R lx_min,
+                              R lx_max, R le) {
+    R u = (le - lx_min) / (lx_max - lx_min);
     R N[4], left[4], right[4];
     N[0] = R(1);
     for (int j = 1; j <= degree; ++j) {
@@ -161,6 +173,12 @@ MIDSX_HD R spline_eval_at(const R* knot_u, const R* ctrl, int degree, int span, 
     R v = R(0);
     for (int i = 0; i <= degree; ++i) v += ctrl[span - degree + i] * N[i];
     return exp10_(v);
+}
+
+template <typename R>
+MIDSX_HD R spline_eval_at(const R* knot_u, const R* ctrl, int degree, int span, R lx_min,
+                          R lx_max, R e) {
+    return spline_eval_at_log(knot_u, ctrl, degree, span, lx_min, lx_max, log10_(e));
 }
 
 // RITA inverse of one energy row: x(y) from the rational interpolation (PENELOPE eq. 1.54

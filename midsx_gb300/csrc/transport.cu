@@ -53,7 +53,13 @@ struct DevSource {
     float f_radius, f_mono;
     const float* f_energy;
     const float* f_cdf;
+    // guide tables of the CDF search (kCdfGuide + 1 entries each, FP64 and FP32 CDF):
+    // guide[k] = lower_bound(cdf, k / kCdfGuide), so lower_bound(cdf, u) for u in
+    // [k / kCdfGuide, (k + 1) / kCdfGuide] lies in [guide[k], guide[k + 1]]
+    const int* guide;
+    const int* f_guide;
 };
+constexpr int kCdfGuide = 256;  // a power of two: k / kCdfGuide and u * kCdfGuide are exact
 
 struct DevGeom {
     double domain[3], origin[3], spacing[3], ext[3];
@@ -306,13 +312,15 @@ __device__ __noinline__ void sample_source(const DevSource& S, HistoryRng& rng, 
         else
             E = S.f_mono;
     } else {
-        // DiscreteInversion::sample: energy[lower_bound(cdf, U)], clamped to the last bin
+        // DiscreteInversion::sample: energy[lower_bound(cdf, U)], clamped to the last bin; the
+        // guide table narrows the search to the nodes between two guide points (same index)
         const R u = uniform<R>(rng);
+        const int g = min(int(u * R(kCdfGuide)), kCdfGuide - 1);
         int idx;
         if constexpr (sizeof(R) == 8)
-            idx = lower_index(S.cdf, 0, S.n_bins, u);
+            idx = lower_index(S.cdf, S.guide[g], S.guide[g + 1], u);
         else
-            idx = lower_index(S.f_cdf, 0, S.n_bins, u);
+            idx = lower_index(S.f_cdf, S.f_guide[g], S.f_guide[g + 1], u);
         if (idx >= S.n_bins) idx = S.n_bins - 1;
         if constexpr (sizeof(R) == 8)
             E = S.energy[idx];
@@ -807,18 +815,36 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
             h[nb + i] = acc;
             s->max_energy = std::max(s->max_energy, spec->bin_energy[i]);
         }
-        // device buffer: FP64 energies and CDF, then their FP32 copies
+        // device buffer: FP64 energies and CDF, their FP32 copies, then the guide tables of
+        // the FP64 and FP32 CDF searches (the same comparison as the device's lower_index; a
+        // CDF that is not monotone keeps the full range in every guide interval)
         std::vector<float> hf(2 * size_t(nb));
         for (size_t i = 0; i < hf.size(); ++i) hf[i] = float(h[i]);
-        CUDA_TRY(cudaMalloc(&s->buf, h.size() * sizeof(double) + hf.size() * sizeof(float)));
+        const bool monotone = std::is_sorted(h.begin() + nb, h.end()) && std::is_sorted(hf.begin() + nb, hf.end());
+        std::vector<int> guide(2 * size_t(kCdfGuide + 1));
+        for (int k = 0; k <= kCdfGuide; ++k) {
+            const double qd = double(k) / kCdfGuide;
+            const float qf = float(k) / float(kCdfGuide);
+            guide[size_t(k)] = monotone ? int(std::lower_bound(h.begin() + nb, h.end(), qd) - (h.begin() + nb))
+                                        : (k == kCdfGuide ? nb : 0);
+            guide[size_t(kCdfGuide + 1 + k)] =
+                monotone ? int(std::lower_bound(hf.begin() + nb, hf.end(), qf) - (hf.begin() + nb))
+                         : (k == kCdfGuide ? nb : 0);
+        }
+        const size_t bytes = h.size() * sizeof(double) + hf.size() * sizeof(float) + guide.size() * sizeof(int);
+        CUDA_TRY(cudaMalloc(&s->buf, bytes));
         CUDA_TRY(cudaMemcpy(s->buf, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
         float* fbuf = reinterpret_cast<float*>(s->buf + h.size());
         CUDA_TRY(cudaMemcpy(fbuf, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice));
+        int* gbuf = reinterpret_cast<int*>(fbuf + hf.size());
+        CUDA_TRY(cudaMemcpy(gbuf, guide.data(), guide.size() * sizeof(int), cudaMemcpyHostToDevice));
         S.n_bins = nb;
         S.energy = s->buf;
         S.cdf = s->buf + nb;
         S.f_energy = fbuf;
         S.f_cdf = fbuf + nb;
+        S.guide = gbuf;
+        S.f_guide = gbuf + kCdfGuide + 1;
     } else {
         if (!(spec->mono_energy > 0)) {
             delete s;
