@@ -237,17 +237,27 @@ midsx_status midsx_gpu_tallies_destroy(midsx_tallies_h t);
 /* Zeroes every accumulator and the run statistics (enqueued on stream). */
 midsx_status midsx_gpu_tallies_reset(midsx_tallies_h t, void* stream);
 
+/* How a warp keeps its lanes busy; results do not depend on it (every history keeps its own
+ * Philox stream).  LANES: each lane holds one history and parks it on an event until
+ * `regroup` lanes wait.  POOL: each warp holds 64 photons in shared memory; a lane whose
+ * photon needs an event takes another at once and the warp runs events 32 at a time. */
+typedef enum midsx_scheduler {
+    MIDSX_SCHED_DEFAULT = 0,
+    MIDSX_SCHED_LANES = 1,
+    MIDSX_SCHED_POOL = 2
+} midsx_scheduler;
+
 typedef struct midsx_run_config {
     int32_t precision;           /* midsx_precision */
     int32_t max_steps;           /* per-history step cap (0 = 100000) */
     int32_t max_compton_trials;  /* Kahn/S(x) rejection cap (0 = 100000) */
     int32_t block_size;          /* 0 = tuned default */
     int32_t blocks_per_sm;       /* 0 = tuned default */
-    int32_t regroup;             /* lanes of a warp parked on an event (real collision, history
-                                    start) before the warp runs its events together (1 = at once;
-                                    0 = tuned default) */
-    int32_t chunk;               /* history ids a lane reserves per fetch (0 = 1) */
-    int32_t reserved;
+    int32_t regroup;             /* events (real collisions, history starts) a warp gathers before
+                                    it runs them together, 1..32 (0 = tuned default) */
+    int32_t chunk;               /* lane-parking scheduler: history ids a lane reserves per fetch
+                                    (0 = 1) */
+    int32_t scheduler;           /* midsx_scheduler */
     uint64_t seed;
     uint64_t first_history;      /* history ids [first, first + n) select Philox streams */
     uint64_t n_histories;
@@ -330,10 +340,10 @@ midsx_status midsx_gpu_batch_run(midsx_batch_h b, const midsx_run_config* cfg, v
  * `stream`; midsx_gpu_batch_replay launches it.  Replays advance the epoch like runs. */
 midsx_status midsx_gpu_batch_capture(midsx_batch_h b, const midsx_run_config* cfg, void* stream);
 midsx_status midsx_gpu_batch_replay(midsx_batch_h b, void* stream);
-/* Times candidate launch shapes (block size, blocks per SM, regroup threshold, histories
- * per fetch) on `trial_histories` histories spread over the jobs in proportion to their
- * sizes, returns the fastest in *best (precision as given) and its histories/s; the trial
- * runs leave the jobs' tallies reset and the epoch unchanged.  Synchronous. */
+/* Times candidate launch shapes (scheduler, block size, blocks per SM, regroup threshold,
+ * histories per fetch) on `trial_histories` histories spread over the jobs in proportion to
+ * their sizes, returns the fastest in *best (precision as given) and its histories/s; the
+ * trial runs leave the jobs' tallies reset and the epoch unchanged.  Synchronous. */
 midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precision, uint64_t trial_histories,
                                       midsx_run_config* best, double* best_rate, void* stream);
 

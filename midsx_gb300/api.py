@@ -293,11 +293,15 @@ class Tallies:
 PRECISIONS = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}
 
 
+SCHEDULERS = {"default": N.SCHED_DEFAULT, "lanes": N.SCHED_LANES, "pool": N.SCHED_POOL}
+
+
 def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0, regroup=0,
-               chunk=0):
+               chunk=0, scheduler="default"):
     c = N.RunConfig()
     c.regroup = int(regroup)
     c.chunk = int(chunk)
+    c.scheduler = SCHEDULERS[scheduler] if isinstance(scheduler, str) else int(scheduler)
     c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     c.n_histories = int(n)
     c.seed = int(seed)
@@ -375,7 +379,8 @@ class Batch:
         rate = C.c_double()
         N.check(N.load().midsx_gpu_batch_autotune(self.handle, PRECISIONS[precision], int(trial), C.byref(best),
                                                   C.byref(rate), stream), "midsx_gpu_batch_autotune")
-        launch = dict(block=best.block_size, per_sm=best.blocks_per_sm, regroup=best.regroup, chunk=best.chunk)
+        launch = dict(block=best.block_size, per_sm=best.blocks_per_sm, regroup=best.regroup, chunk=best.chunk,
+                      scheduler=best.scheduler)
         return launch, rate.value
 
     def close(self):

@@ -1,0 +1,474 @@
+// kernel_pool.cuh - the transport kernel with a per-warp photon pool (included by transport.cu
+// after kernel_body.cuh, whose device functions it shares).
+//
+// Each warp owns kPoolSlots photon slots in shared memory, two per lane: the state a photon
+// carries between events (position, direction, energy, Philox position, scatter counts,
+// history counters) and its per-energy cache (majorant, every material's total cross section
+// and delta threshold).  Each lane steps one photon - the Woodcock step of
+// src/MIDSX/Core/physics_engine.cpp:28-79.  A photon that needs an event (a real collision, or
+// a new history after its end) is parked in the warp's event list and the lane takes a photon
+// from the warp's ready list at once, so the warp keeps stepping with all its lanes while
+// events accumulate.  Once `regroup` events wait - or nothing is left to step - the warp runs
+// up to 32 of them together, one per lane, and returns the surviving photons and the new
+// histories to the ready list.
+//
+// Scheduling does not enter the physics: each history draws from its own Philox stream in the
+// same order as in the lane-parking kernel, so the two kernels give the same trajectories, and
+// bit-identical integer tallies in the mixed form.  Everything is warp-synchronous: a warp
+// never waits for another warp, and the loop ends when the warp's lanes, ready list and event
+// list are all empty after the launch's histories are handed out.
+
+constexpr int kPoolSlots = 64;        // photon slots per warp
+constexpr uint32_t kKindFlight = 0u;  // slot kinds (meta bits 30-31)
+constexpr uint32_t kKindCollide = 1u;
+constexpr uint32_t kKindStart = 2u;
+
+// meta word of a slot: job (bits 0-7), material (8-15), coherent (16-22) and incoherent
+// (23-29) scatter counts saturated at 127 (only 0, 1 and "more" matter: scatter_class), kind.
+__device__ __forceinline__ uint32_t pack_meta(int job, int mat, int n_coh, int n_incoh, uint32_t kind) {
+    return uint32_t(job) | (uint32_t(mat) << 8) | (uint32_t(min(n_coh, 127)) << 16) |
+           (uint32_t(min(n_incoh, 127)) << 23) | (kind << 30);
+}
+
+// Shared-memory arrays over the block's slots (structure of arrays: lanes touch consecutive
+// words when they hold consecutive slots).
+template <typename R>
+struct PoolSlots {
+    R *px, *py, *pz, *dx, *dy, *dz, *e, *mumax, *qx, *qy, *qz, *s;  // q = start of the last step
+    uint32_t *rn, *h0, *h1, *steps, *fetches, *words, *vox, *meta;
+    R *thr, *mu;  // per-energy cache, [material][slot]
+};
+
+constexpr int kPoolRealWords = 12;  // R arrays per slot
+constexpr int kPoolIntWords = 8;    // uint32 arrays per slot
+
+template <typename R>
+__host__ __device__ inline size_t pool_head_bytes(int n_jobs, bool multi) {
+    size_t b = size_t(n_jobs) * kStCount * 8;
+    if (multi) b += size_t(n_jobs + 1) * 8 + size_t(n_jobs) * sizeof(Geo<R>);
+    return (b + 15) & ~size_t(15);
+}
+
+// Shared-memory bytes of a pool launch: per-job counters, batch prefix and geometry, the
+// slots, then each warp's ready and event lists (one byte per entry).
+template <typename R>
+__host__ __device__ inline size_t pool_smem(int n_jobs, bool multi, int n_materials, int block) {
+    const size_t ns = size_t(block / 32) * kPoolSlots;
+    size_t b = pool_head_bytes<R>(n_jobs, multi);
+    b += ns * (kPoolRealWords * sizeof(R) + kPoolIntWords * 4 + 2 * size_t(n_materials) * sizeof(R));
+    b = (b + 15) & ~size_t(15);
+    return b + size_t(block / 32) * 2 * kPoolSlots;
+}
+
+template <typename R, bool MULTI>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_kernel(const RunParams P) {
+    constexpr bool MX = sizeof(R) == 4;
+    constexpr unsigned FULL = 0xffffffffu;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int njobs = MULTI ? P.n_jobs : 1;
+    const int M = P.T.n_materials;
+    unsigned long long* s_stats = reinterpret_cast<unsigned long long*>(smem_raw);
+    unsigned long long* s_prefix = s_stats + njobs * kStCount;
+    Geo<R>* s_geo = reinterpret_cast<Geo<R>*>(s_prefix + (MULTI ? njobs + 1 : 0));
+    const int nw = int(blockDim.x >> 5);
+    const int ns = nw * kPoolSlots;
+    PoolSlots<R> S;
+    {
+        unsigned char* p = smem_raw + pool_head_bytes<R>(njobs, MULTI);
+        R** reals[kPoolRealWords] = {&S.px, &S.py, &S.pz, &S.dx, &S.dy, &S.dz, &S.e, &S.mumax,
+                                     &S.qx, &S.qy, &S.qz, &S.s};
+        for (int i = 0; i < kPoolRealWords; ++i) {
+            *reals[i] = reinterpret_cast<R*>(p);
+            p += size_t(ns) * sizeof(R);
+        }
+        S.thr = reinterpret_cast<R*>(p);
+        p += size_t(ns) * M * sizeof(R);
+        S.mu = reinterpret_cast<R*>(p);
+        p += size_t(ns) * M * sizeof(R);
+        uint32_t** ints[kPoolIntWords] = {&S.rn, &S.h0, &S.h1, &S.steps, &S.fetches, &S.words, &S.vox, &S.meta};
+        for (int i = 0; i < kPoolIntWords; ++i) {
+            *ints[i] = reinterpret_cast<uint32_t*>(p);
+            p += size_t(ns) * 4;
+        }
+    }
+    uint8_t* stacks = smem_raw + pool_smem<R>(njobs, MULTI, M, int(blockDim.x)) - size_t(nw) * 2 * kPoolSlots;
+    for (int i = threadIdx.x; i < njobs * kStCount; i += blockDim.x) s_stats[i] = 0;
+    if (MULTI) {
+        for (int i = threadIdx.x; i <= njobs; i += blockDim.x) s_prefix[i] = P.prefix[i];
+        for (int i = threadIdx.x; i < njobs; i += blockDim.x) s_geo[i] = make_geo<R>(P.jobs[i].G);
+    }
+    const unsigned lane = threadIdx.x & 31u;
+    const int warp = int(threadIdx.x >> 5);
+    const unsigned below = (1u << lane) - 1u;
+    const int sbase = warp * kPoolSlots;
+    uint8_t* rdy = stacks + warp * 2 * kPoolSlots;  // ready list: slots to step
+    uint8_t* evq = rdy + kPoolSlots;               // event list: slots waiting for an event
+    // every slot starts as a history start
+    evq[lane] = uint8_t(lane);
+    evq[lane + 32] = uint8_t(lane + 32);
+    S.meta[sbase + lane] = pack_meta(0, 0, 0, 0, kKindStart);
+    S.meta[sbase + lane + 32] = pack_meta(0, 0, 0, 0, kKindStart);
+    __syncthreads();
+    const Geo<R> g0 = make_geo<R>(P.job0.G);
+    const unsigned long long epoch = P.epoch ? *P.epoch : 0ull;
+    const int regroup = max(1, min(P.regroup, 32));
+    int rdy_top = 0, ev_top = kPoolSlots;  // warp-uniform list sizes
+    bool exhausted = false;                // warp-uniform: every history of the launch handed out
+
+    // the photon in this lane's registers
+    int cur = -1;  // slot stepped by this lane
+    V3<R> pos, dir, p0;
+    R E = R(0), mu_max = R(1), inv_mu_max = R(1), s = R(0);
+    HistoryRng rng;
+    int job = 0, mat = 0, vox = -1, n_coh = 0, n_incoh = 0, ntal = 0;
+    uint32_t kind = kKindFlight, steps = 0, fetches = 0, trials = 0, words = 0;
+
+    // Slot traffic is kept to the fields each transition needs.  In flight a photon changes
+    // only its position, Philox position and counters; the collision site (step start, length,
+    // voxel, material) matters only to the event that follows.
+    auto load_flight = [&](int sl) {  // what a step needs
+        pos = {S.px[sl], S.py[sl], S.pz[sl]};
+        dir = {S.dx[sl], S.dy[sl], S.dz[sl]};
+        E = S.e[sl];
+        mu_max = S.mumax[sl];
+        inv_mu_max = R(1) / mu_max;
+        const uint32_t meta = S.meta[sl];
+        job = int(meta & 0xffu);
+        n_coh = int((meta >> 16) & 0x7fu);
+        n_incoh = int((meta >> 23) & 0x7fu);
+        kind = meta >> 30;
+        const uint64_t seed = MULTI ? P.jobs[job].seed : P.job0.seed;
+        rng.k0 = uint32_t(seed);
+        rng.k1 = uint32_t(seed >> 32);
+        rng.h0 = S.h0[sl];
+        rng.h1 = S.h1[sl];
+        rng.n = S.rn[sl];
+        // the unused half of a Philox block is never drawn after an event: the next step
+        // starts a new block (HistoryRng::next_pair64)
+        rng.b0 = rng.b1 = 0u;
+        steps = S.steps[sl];
+        fetches = S.fetches[sl];
+        words = S.words[sl];
+        ntal = MULTI ? P.jobs[job].n_tallies : P.job0.n_tallies;
+    };
+    auto load_event = [&](int sl) {  // a parked photon: flight state plus its collision site
+        load_flight(sl);
+        p0 = {S.qx[sl], S.qy[sl], S.qz[sl]};
+        s = S.s[sl];
+        mat = int((S.meta[sl] >> 8) & 0xffu);
+        vox = int(S.vox[sl]);
+    };
+    auto save_flight = [&](int sl) {  // what a step changes
+        S.px[sl] = pos.x;
+        S.py[sl] = pos.y;
+        S.pz[sl] = pos.z;
+        S.rn[sl] = rng.n;
+        S.steps[sl] = steps;
+        S.fetches[sl] = fetches;
+        S.words[sl] = words;
+    };
+    auto save_collision = [&](int sl) {  // a photon parked at a real collision
+        save_flight(sl);
+        S.qx[sl] = p0.x;
+        S.qy[sl] = p0.y;
+        S.qz[sl] = p0.z;
+        S.s[sl] = s;
+        S.vox[sl] = uint32_t(vox);
+        S.meta[sl] = pack_meta(job, mat, n_coh, n_incoh, kKindCollide);
+    };
+    auto save_after_event = [&](int sl) {  // a photon leaving an event (or a new history)
+        save_flight(sl);
+        S.dx[sl] = dir.x;
+        S.dy[sl] = dir.y;
+        S.dz[sl] = dir.z;
+        S.e[sl] = E;
+        S.mumax[sl] = mu_max;
+        S.h0[sl] = rng.h0;
+        S.h1[sl] = rng.h1;
+        S.meta[sl] = pack_meta(job, mat, n_coh, n_incoh, kKindFlight);
+    };
+    // Compton trials go to the statistics at the event itself (sample_compton counts them)
+    auto end_history = [&]() {
+        unsigned long long* st = s_stats + job * kStCount;
+        stat_add(st, kStSteps, steps);
+        stat_add(st, kStFetches, fetches);
+        stat_add(st, kStWords, words);
+    };
+
+    for (;;) {
+        // lanes without a photon take one from the ready list
+        {
+            const bool want = cur < 0;
+            const unsigned wm = __ballot_sync(FULL, want);
+            const int r = __popc(wm & below);
+            if (want && r < rdy_top) {
+                cur = sbase + rdy[rdy_top - 1 - r];
+                load_flight(cur);
+            }
+            rdy_top -= min(__popc(wm), rdy_top);
+        }
+        if (__ballot_sync(FULL, cur >= 0) == 0u && rdy_top == 0 && ev_top == 0) break;
+        uint32_t park = kKindFlight;
+        if (cur >= 0) {
+            // one Woodcock step: getFreePath, move, domain test, voxel fetch, isDeltaScatter
+            const Geo<R>& g = MULTI ? s_geo[job] : g0;
+            unsigned long long* st = s_stats + job * kStCount;
+            if (steps >= uint32_t(P.max_steps)) {
+                stat_add(st, kStStepCap, 1);
+                end_history();
+                park = kKindStart;
+            } else {
+                ++steps;
+                uint64_t w1, w2;
+                rng.next_pair64(w1, w2);
+                if constexpr (MX)
+                    s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) * inv_mu_max;
+                else
+                    s = -log_(to_uniform(w1, R(0))) / mu_max;
+                p0 = pos;
+                pos = {pos.x + s * dir.x, pos.y + s * dir.y, pos.z + s * dir.z};
+                if (!(pos.x >= R(0) && pos.x <= g.dom.x && pos.y >= R(0) && pos.y <= g.dom.y && pos.z >= R(0) &&
+                      pos.z <= g.dom.z)) {
+                    if (ntal) {
+                        const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
+                        score_tallies<R, MX>(tal, ntal, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false, R(0),
+                                             words);
+                    }
+                    stat_add(st, kStEscE, fx_stat(E));
+                    end_history();
+                    park = kKindStart;
+                } else {
+                    const V3<R> q = {pos.x - g.org.x, pos.y - g.org.y, pos.z - g.org.z};
+                    vox = -1;
+                    mat = g.bg;
+                    if (q.x >= R(0) && q.x <= g.ext.x && q.y >= R(0) && q.y <= g.ext.y && q.z >= R(0) &&
+                        q.z <= g.ext.z) {
+                        int ix, iy, iz;
+                        if constexpr (MX) {
+                            ix = int(q.x * g.ispc.x);
+                            iy = int(q.y * g.ispc.y);
+                            iz = int(q.z * g.ispc.z);
+                        } else {
+                            ix = int(q.x / g.spc.x);
+                            iy = int(q.y / g.spc.y);
+                            iz = int(q.z / g.spc.z);
+                        }
+                        if (ix >= g.nx || iy >= g.ny || iz >= g.nz) {
+                            stat_add(st, kStEdge, 1);  // the reference's vector::at would throw here
+                            ix = min(ix, g.nx - 1);
+                            iy = min(iy, g.ny - 1);
+                            iz = min(iz, g.nz - 1);
+                        }
+                        vox = ix + iy * g.nx + iz * g.nx * g.ny;
+                        mat = __ldg(g.ids + vox);
+                        ++fetches;
+                    }
+                    if (to_uniform(w2, R(0)) < S.thr[mat * ns + cur]) {
+                        if (ntal) {
+                            const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
+                            score_tallies<R, MX>(tal, ntal, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false,
+                                                 R(0), words);
+                        }
+                    } else {
+                        park = kKindCollide;  // a real collision
+                    }
+                }
+            }
+        }
+        // photons that need an event go to the event list
+        {
+            const bool parks = park != kKindFlight;
+            const unsigned pm = __ballot_sync(FULL, parks);
+            if (parks) {
+                if (park == kKindCollide)
+                    save_collision(cur);
+                else
+                    S.meta[cur] = pack_meta(0, 0, 0, 0, kKindStart);
+                evq[ev_top + __popc(pm & below)] = uint8_t(cur - sbase);
+                cur = -1;
+            }
+            ev_top += __popc(pm);
+        }
+        __syncwarp();
+        const bool idle = __ballot_sync(FULL, cur >= 0) == 0u;
+        if (!(ev_top >= regroup || (idle && rdy_top == 0 && ev_top > 0))) continue;
+
+        // ------------------------------------------------------------ event phase ---
+        if (cur >= 0) save_flight(cur);  // the stepping photons wait in their slots
+        __syncwarp();
+        const int n_ev = min(ev_top, 32);
+        int sl = int(lane) < n_ev ? sbase + evq[ev_top - 1 - int(lane)] : -1;
+        ev_top -= n_ev;
+        bool need_start = false, need_refresh = false;
+        if (sl >= 0) {
+            load_event(sl);
+            if (kind != kKindCollide) {
+                need_start = true;
+            } else {
+                unsigned long long* st = s_stats + job * kStCount;
+                bool finish = false;
+                // setInteractionType (physics_engine.cpp:82-109)
+                const DevMaterial& Mt = P.T.mat[mat];
+                const R mu_tot = S.mu[mat * ns + sl];
+                R p_coh, p_incoh;
+                interaction_probs<R>(P.T, Mt, E, mu_tot, p_coh, p_incoh);
+                const R u3 = uniform<R>(rng);
+                const int cls0 = scatter_class(n_coh, n_incoh);
+                const R E0 = E;
+                const V3<R> d0 = dir;
+                R dep = R(0), mu_s = R(1);
+                bool energy_changed = false, failed = false, scattered = false;
+                if (u3 < p_coh) {
+                    // CoherentScattering::interact
+                    ++n_coh;
+                    stat_add(st, kStCoh, 1);
+                    R mu;
+                    if (!rita_sample<R>(P.T, Mt.rita, E, uniform<R>(rng), mu)) {
+                        stat_add(st, kStRangeErr, 1);
+                        failed = true;
+                    } else {
+                        mu_s = mu;
+                        scattered = true;
+                    }
+                } else if (u3 < p_coh + p_incoh) {
+                    // IncoherentScattering::interact
+                    ++n_incoh;
+                    stat_add(st, kStIncoh, 1);
+                    R mu = R(1), kp = E / R(kMec2);
+                    trials = 0;
+                    const bool sampled = sample_compton<R>(P, Mt, rng, E, mu, kp, trials);
+                    stat_add(st, kStTrials, trials);
+                    if (!sampled) {
+                        stat_add(st, kStTrialCap, 1);
+                        failed = true;
+                    } else {
+                        const R k = E / R(kMec2);
+                        mu_s = mu;
+                        scattered = true;
+                        E = kp * R(kMec2);
+                        dep = R(kMec2) * (k - kp);
+                        energy_changed = true;
+                    }
+                } else {
+                    // PhotoelectricEffect::interact
+                    stat_add(st, kStPhoto, 1);
+                    dep = E;
+                    finish = true;
+                }
+                // both scatterings end with the new direction (azimuth drawn last, as in each
+                // interaction's own order): one call serves the coherent and incoherent lanes
+                if (scattered) dir = scatter_dir(dir, mu_s, uniform<R>(rng));
+                if (failed) {
+                    finish = true;
+                } else {
+                    if (ntal) {
+                        const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
+                        score_tallies<R, MX>(tal, ntal, p0, d0, s, E0, cls0, scatter_class(n_coh, n_incoh), true, dep,
+                                             words);
+                    }
+                    if (dep != R(0)) {
+                        if (vox >= 0) {
+                            stat_add(st, kStDepGrid, fx_stat(dep));
+                            const DevJob& J = MULTI ? P.jobs[job] : P.job0;
+                            if (J.dose_stride) {
+                                score_dose<R, MX>(J.dose, J.dose_stride, vox, dep);
+                                ++words;
+                            }
+                        } else {
+                            stat_add(st, kStDepBg, fx_stat(dep));
+                        }
+                    }
+                    if (!finish) {
+                        if (!(fabs_(dir.x) <= R(2) && fabs_(dir.y) <= R(2) && fabs_(dir.z) <= R(2))) {
+                            // a NaN direction (RITA rows below ~400 eV are NaN, as in the
+                            // reference); its next step would leave the domain: retire the history
+                            stat_add(st, kStNonFinite, 1);
+                            stat_add(st, kStEscE, fx_stat(E));
+                            finish = true;
+                        } else if (energy_changed) {
+                            need_refresh = true;
+                        }
+                    }
+                }
+                if (finish) {
+                    end_history();
+                    need_start = true;
+                }
+            }
+        }
+        // new histories: one atomic per warp hands out the lanes' history indices
+        const unsigned nm = __ballot_sync(FULL, need_start);
+        if (nm) {
+            unsigned long long base = P.total;
+            if (!exhausted) {
+                const int leader = __ffs(nm) - 1;
+                if (int(lane) == leader) base = atomicAdd(P.counter, (unsigned long long)__popc(nm));
+                base = __shfl_sync(FULL, base, leader);
+                if (base + (unsigned long long)__popc(nm) >= P.total) exhausted = true;
+            }
+            if (need_start) {
+                const unsigned long long gidx = base + (unsigned long long)__popc(nm & below);
+                if (gidx >= P.total) {
+                    sl = -1;  // nothing left to start: the slot stays empty
+                } else {
+                    uint64_t seed, hid;
+                    if (MULTI) {
+                        int lo = 0, hi = njobs;  // last job with prefix <= gidx
+                        while (hi - lo > 1) {
+                            const int mid = (lo + hi) >> 1;
+                            if (s_prefix[mid] <= gidx) lo = mid;
+                            else hi = mid;
+                        }
+                        job = lo;
+                        const DevJob& J = P.jobs[job];
+                        seed = J.seed;
+                        hid = J.first + epoch * J.n + (gidx - s_prefix[job]);
+                        ntal = J.n_tallies;
+                    } else {
+                        job = 0;
+                        seed = P.job0.seed;
+                        hid = P.job0.first + epoch * P.job0.n + gidx;
+                        ntal = P.job0.n_tallies;
+                    }
+                    // PhotonSource::generatePhoton + a fresh per-history stream
+                    rng.init(seed, hid);
+                    sample_source<R>(MULTI ? P.jobs[job].S : P.job0.S, rng, pos, dir, E);
+                    unsigned long long* sj = s_stats + job * kStCount;
+                    stat_add(sj, kStHistories, 1);
+                    stat_add(sj, kStSourceE, fx_stat(E));
+                    n_coh = n_incoh = 0;
+                    steps = fetches = trials = words = 0;
+                    mat = 0;
+                    vox = -1;
+                    s = R(0);
+                    p0 = pos;
+                    need_refresh = true;
+                }
+            }
+        }
+        // per-energy cache of Compton survivors and new histories, in one call
+        if (need_refresh) {
+            mu_max = refresh_energy<R>(P, E, S.thr + sl, S.mu + sl, ns);
+            inv_mu_max = R(1) / mu_max;
+        }
+        // survivors and new histories go to the ready list
+        {
+            const bool ready = sl >= 0;
+            if (ready) save_after_event(sl);
+            const unsigned rm = __ballot_sync(FULL, ready);
+            if (ready) rdy[rdy_top + __popc(rm & below)] = uint8_t(sl - sbase);
+            rdy_top += __popc(rm);
+        }
+        __syncwarp();
+        if (cur >= 0) load_flight(cur);  // back to the photon this lane was stepping
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < njobs * kStCount; i += blockDim.x) {
+        const unsigned long long v = s_stats[i];
+        if (v) {
+            const int j = i / kStCount;
+            unsigned long long* dst = MULTI ? P.jobs[j].stats : P.job0.stats;
+            atomicAdd(dst + (i - j * kStCount), v);
+        }
+    }
+}

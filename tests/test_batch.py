@@ -98,7 +98,11 @@ def test_autotune_picks_a_shape_and_resets_tallies(setup):
     batch = M.Batch(tables, [(ph, src, tl, 1, 0, sc.n_histories) for sc, (ph, src, tl) in zip(jobs, objs)])
     launch, rate = batch.autotune("mixed", trial=200_000)
     assert rate > 0
-    assert launch["block"] in (128, 256) and 12 <= launch["regroup"] <= 28 and launch["chunk"] in (1, 4)
+    if launch["scheduler"] == N.SCHED_POOL:
+        assert launch["block"] in (64, 96, 128) and 24 <= launch["regroup"] <= 32
+    else:
+        assert launch["scheduler"] == N.SCHED_LANES
+        assert launch["block"] in (128, 256) and 12 <= launch["regroup"] <= 28 and launch["chunk"] in (1, 4)
     for ph, src, tl in objs:
         assert tl.dose()["sum"].sum() == 0 and tl.stats()["histories"] == 0
     batch.run("mixed", **launch)
