@@ -292,10 +292,11 @@ def main():
     if os.path.exists(peaks_path):
         peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "transport_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "transport_traffic.txt")
     if os.path.exists(tpath):
-        t = json.load(open(tpath))
-        traffic = float(t["dram_bytes_per_history"]) * N_hist
+        for line in open(tpath):
+            if line.startswith("dram_bytes_per_history"):
+                traffic = float(line.split()[1]) * N_hist
     result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                           "bytes_per_history": b_hist, "F": F, "W": W,

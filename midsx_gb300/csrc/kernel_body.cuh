@@ -21,7 +21,7 @@
 // per-energy cache: majorant and every material's total cross section and delta-scatter
 // threshold (isDeltaScatter: p_delta = 1 - mu / mu_max), kept per thread in shared memory
 template <typename R>
-__device__ __noinline__ R refresh_energy(const RunParams& P, R E, R* thr, R* mu, int stride) {
+__device__ __forceinline__ R refresh_energy(const RunParams& P, R E, R* thr, R* mu, int stride) {
     const EnergyKey<R> key = energy_key<R>(P.T, E);  // one log10 and bucket for every table
     R mu_max = lin_lookup_key<R>(P.T, P.T.majorant, key);
     for (int m = 0; m < P.T.n_materials; ++m) {
@@ -39,8 +39,16 @@ template <typename R>
 __device__ __forceinline__ void interaction_probs(const DevTables& T, const DevMaterial& Mt, R E, R mu_tot, R& p_coh,
                                                R& p_incoh) {
     const EnergyKey<R> key = energy_key<R>(T, E);
-    p_coh = spline_lookup_key<R>(T, Mt.coh, key) / mu_tot;
-    p_incoh = spline_lookup_key<R>(T, Mt.incoh, key) / mu_tot;
+    // one copy of the spline evaluation, run for both cross sections
+    R coh = R(0), incoh = R(0);
+#pragma unroll 1
+    for (int w = 0; w < 2; ++w) {
+        const R v = spline_lookup_key<R>(T, w ? Mt.incoh : Mt.coh, key);
+        if (w) incoh = v;
+        else coh = v;
+    }
+    p_coh = coh / mu_tot;
+    p_incoh = incoh / mu_tot;
 }
 
 // scatter_direction for the coherent and incoherent branches.
@@ -52,7 +60,7 @@ __device__ __forceinline__ V3<R> scatter_dir(const V3<R>& v, R mu, R u) {
 // Compton scattering by Kahn's method with the S(x) rejection
 // (src/MIDSX/Core/photon_interactions.cpp:62-141).  Returns false at the trial cap.
 template <typename R>
-__device__ __noinline__ bool sample_compton(const RunParams& P, const DevMaterial& Mt, HistoryRng& rng, R E, R& mu,
+__device__ __forceinline__ bool sample_compton(const RunParams& P, const DevMaterial& Mt, HistoryRng& rng, R E, R& mu,
                                             R& kp, uint32_t& trials) {
     R alpha;
     if constexpr (sizeof(R) == 8)
@@ -84,7 +92,7 @@ __device__ __noinline__ bool sample_compton(const RunParams& P, const DevMateria
 }
 
 template <typename R, bool MX>
-__device__ __noinline__ void score_dose(unsigned long long* dose, int stride, int vox, R dep) {
+__device__ __forceinline__ void score_dose(unsigned long long* dose, int stride, int vox, R dep) {
     unsigned long long* rec = dose + size_t(vox) * stride;
     Acc<MX>::energy(rec, dep);
     if (stride > 1) {

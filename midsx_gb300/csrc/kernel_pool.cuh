@@ -213,9 +213,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
             // one Woodcock step: getFreePath, move, domain test, voxel fetch, isDeltaScatter
             const Geo<R>& g = MULTI ? s_geo[job] : g0;
             unsigned long long* st = s_stats + job * kStCount;
+            bool segment = false;  // the step's segment goes to the tallies (escape or delta step)
             if (steps >= uint32_t(P.max_steps)) {
                 stat_add(st, kStStepCap, 1);
-                end_history();
                 park = kKindStart;
             } else {
                 ++steps;
@@ -229,13 +229,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                 pos = {pos.x + s * dir.x, pos.y + s * dir.y, pos.z + s * dir.z};
                 if (!(pos.x >= R(0) && pos.x <= g.dom.x && pos.y >= R(0) && pos.y <= g.dom.y && pos.z >= R(0) &&
                       pos.z <= g.dom.z)) {
-                    if (ntal) {
-                        const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
-                        score_tallies<R, MX>(tal, ntal, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false, R(0),
-                                             words);
-                    }
                     stat_add(st, kStEscE, fx_stat(E));
-                    end_history();
+                    segment = true;
                     park = kKindStart;
                 } else {
                     const V3<R> q = {pos.x - g.org.x, pos.y - g.org.y, pos.z - g.org.z};
@@ -263,17 +258,19 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                         mat = __ldg(g.ids + vox);
                         ++fetches;
                     }
-                    if (to_uniform(w2, R(0)) < S.thr[mat * ns + cur]) {
-                        if (ntal) {
-                            const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
-                            score_tallies<R, MX>(tal, ntal, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false,
-                                                 R(0), words);
-                        }
-                    } else {
+                    if (to_uniform(w2, R(0)) < S.thr[mat * ns + cur])
+                        segment = true;
+                    else
                         park = kKindCollide;  // a real collision
-                    }
                 }
             }
+            // surface and volume tallies see every step that does not interact, the last
+            // (escaping) one included (physics_engine.cpp:48-49)
+            if (segment && ntal) {
+                const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
+                score_tallies<R, MX>(tal, ntal, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false, R(0), words);
+            }
+            if (park == kKindStart) end_history();
         }
         // photons that need an event go to the event list
         {

@@ -167,7 +167,7 @@ __device__ __forceinline__ void vec_cosine(unsigned long long* acc, int q, int c
 // cls1: class of final_photon (post-interaction counts if the step interacted, else
 // a default Photon = primary), used by volume quantities.
 template <typename R, bool MX>
-__device__ __noinline__ void score_tallies(const DevTally* tallies, int n_tallies, const V3<R>& p0, const V3<R>& d,
+__device__ __forceinline__ void score_tallies(const DevTally* tallies, int n_tallies, const V3<R>& p0, const V3<R>& d,
                                            R s, R E, int cls0, int cls1, bool interact, R dep, uint32_t& words) {
     for (int ti = 0; ti < n_tallies; ++ti) {
         const DevTally& T = tallies[ti];
@@ -268,7 +268,7 @@ __device__ __forceinline__ V3<R> src3(const double* d, const float* f) {
 }
 
 template <typename R>
-__device__ __noinline__ void sample_source(const DevSource& S, HistoryRng& rng, V3<R>& pos, V3<R>& dir, R& E) {
+__device__ __forceinline__ void sample_source(const DevSource& S, HistoryRng& rng, V3<R>& pos, V3<R>& dir, R& E) {
     pos = src3<R>(S.pos, S.f_pos);
     const V3<R> A = src3<R>(S.a, S.f_a), B = src3<R>(S.b, S.f_b), Cc = src3<R>(S.c, S.f_c);
     V3<R> d;
