@@ -168,6 +168,23 @@ midsx_status midsx_gpu_phantom_create(midsx_tables_h tables, const midsx_geometr
                                       const uint8_t* ids, midsx_phantom_h* out);
 midsx_status midsx_gpu_phantom_destroy(midsx_phantom_h p);
 
+/* A domain with several voxel grids: ComputationalDomain's voxel_grids_
+ * (src/MIDSX/Core/computational_domain.cpp:23-31, 92-104).  A point belongs to the first grid,
+ * in the given order, whose closed box [origin, origin + dims * spacing] holds it, else to the
+ * background material.  The phantom's voxels are numbered grid after grid (grid g's voxels
+ * follow all voxels of grids 0..g-1), which is the layout of its dose tally. */
+#define MIDSX_MAX_GRIDS 16
+typedef struct midsx_grid_spec {
+    double spacing[3];
+    double origin[3];        /* lower corner in the domain (cm) */
+    int32_t dims[3];
+    int32_t reserved;
+    const uint8_t* ids;      /* host memory: dims[0]*dims[1]*dims[2] MIDSX ids, x fastest */
+} midsx_grid_spec;
+
+midsx_status midsx_gpu_phantom_create_grids(midsx_tables_h tables, const double* domain, int32_t background_id,
+                                            const midsx_grid_spec* grids, int32_t n_grids, midsx_phantom_h* out);
+
 /* PhotonSource (src/MIDSX/Core/source.cpp:44-155).  Geometry is a point (PointGeometry).
  * Directionality:
  *   BEAM:        a = pass-through point

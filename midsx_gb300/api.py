@@ -130,10 +130,40 @@ class Phantom:
         N.check(lib.midsx_gpu_phantom_create(tables.handle, C.byref(self.spec), ids.ctypes.data, C.byref(h)),
                 "midsx_gpu_phantom_create")
         self.handle = h
+        self.grid_shapes = [ids.shape]
+
+    @classmethod
+    def from_grids(cls, tables, domain, background_id, grids):
+        """A domain with several voxel grids (ComputationalDomain's voxel_grids_): grids is a
+        list of (ids shaped (nz, ny, nx), spacing, origin).  A point belongs to the first grid
+        in the list whose closed box holds it; voxels are numbered grid after grid."""
+        self = cls.__new__(cls)
+        arr = (N.GridSpec * len(grids))()
+        self._grid_ids = []
+        for k, (ids, spacing, origin) in enumerate(grids):
+            ids = np.ascontiguousarray(ids, dtype=np.uint8)
+            if ids.ndim != 3:
+                raise ValueError("ids must be 3-D arrays shaped (nz, ny, nx)")
+            nz, ny, nx = ids.shape
+            arr[k].spacing, arr[k].origin = N.vec3(spacing), N.vec3(origin)
+            arr[k].dims = N.I3(nx, ny, nz)
+            arr[k].ids = ids.ctypes.data
+            self._grid_ids.append(ids)
+        dom = (C.c_double * 3)(*[float(x) for x in domain])
+        h = C.c_void_p()
+        self.handle = None
+        N.check(N.load().midsx_gpu_phantom_create_grids(tables.handle, dom, int(background_id), arr, len(grids),
+                                                        C.byref(h)), "midsx_gpu_phantom_create_grids")
+        self.handle = h
+        self.ids = self._grid_ids[0]
+        self.dims = tuple(reversed(self.ids.shape))
+        self.grid_shapes = [a.shape for a in self._grid_ids]
+        self.spec = None
+        return self
 
     @property
     def n_voxels(self):
-        return int(np.prod(self.dims))
+        return int(sum(np.prod(sh) for sh in self.grid_shapes))
 
     def close(self):
         if self.handle:
@@ -231,7 +261,7 @@ class Tallies:
         self.specs = list(specs)
         self.dose_mode = dose_mode
         self.phantom = phantom
-        self.shape = phantom.ids.shape if phantom is not None else None
+        self.shapes = list(phantom.grid_shapes) if phantom is not None else None
         arr = tally_specs(self.specs)
         lib = N.load()
         h = C.c_void_p()
@@ -250,18 +280,29 @@ class Tallies:
         return st.as_dict()
 
     def dose(self, stream=None):
-        n = int(np.prod(self.shape))
+        """Per-voxel dose records: arrays shaped like the phantom's grid, or, for a phantom of
+        several grids, lists with one array per grid."""
+        n = int(sum(np.prod(sh) for sh in self.shapes))
         s = np.empty(n)
         full = self.dose_mode == N.DOSE_FULL
         s2 = np.empty(n) if full else None
         c = np.empty(n) if full else None
         N.check(N.load().midsx_gpu_fetch_dose(self.handle, N.dptr(s), N.dptr(s2) if full else None,
                                               N.dptr(c) if full else None, stream), "midsx_gpu_fetch_dose")
-        shape = self.shape
-        out = {"sum": s.reshape(shape)}
+        def shaped(a):
+            if len(self.shapes) == 1:
+                return a.reshape(self.shapes[0])
+            parts, off = [], 0
+            for sh in self.shapes:
+                k = int(np.prod(sh))
+                parts.append(a[off:off + k].reshape(sh))
+                off += k
+            return parts
+
+        out = {"sum": shaped(s)}
         if full:
-            out["sumsq"] = s2.reshape(shape)
-            out["count"] = c.reshape(shape)
+            out["sumsq"] = shaped(s2)
+            out["count"] = shaped(c)
         return out
 
     def scalar(self, i, stream=None):
@@ -441,7 +482,7 @@ class TallyView(Tallies):
 
     def __init__(self, handle, shape, specs=(), dose_mode=N.DOSE_FULL):
         self.handle = handle
-        self.shape = shape
+        self.shapes = [shape]
         self.specs = list(specs)
         self.dose_mode = dose_mode
         self.phantom = None

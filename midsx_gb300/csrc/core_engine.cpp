@@ -50,24 +50,33 @@ void PhysicsEngine::addSurfaceTallies(std::vector<std::unique_ptr<SurfaceTally>>
 void PhysicsEngine::ensureDevice() {
     if (dev_) return;
     if (!interaction_data_.blob()) throw std::invalid_argument("InteractionData has no materials");
-    if (comp_domain_.getNumVoxelGrids() != 1)
-        throw std::invalid_argument("the GPU transport takes a ComputationalDomain with exactly one voxel grid");
+    const int n_grids = comp_domain_.getNumVoxelGrids();
+    if (n_grids < 1 || n_grids > MIDSX_MAX_GRIDS)
+        throw std::invalid_argument("the GPU transport takes a ComputationalDomain with 1 to 16 voxel grids");
     auto d = std::make_unique<Device>();
     check(midsx_gpu_tables_create(interaction_data_.blob(), &d->tables), "midsx_gpu_tables_create");
-    VoxelGrid& g = comp_domain_.getVoxelGridN(0);
-    midsx_geometry_spec geom;
-    std::memset(&geom, 0, sizeof(geom));
-    Vec3 dom = comp_domain_.getDimSpace(), org = comp_domain_.getVoxelGridOriginN(0), sp = g.getSpacing();
-    VoxelIndex dims = g.getDimVox();
-    for (int i = 0; i < 3; ++i) {
-        geom.domain[i] = dom(i);
-        geom.origin[i] = org(i);
-        geom.spacing[i] = sp(i);
-        geom.dims[i] = dims[size_t(i)];
+    // every grid, in the domain's order (getVoxel's first-hit order)
+    std::vector<std::vector<uint8_t>> ids(static_cast<size_t>(n_grids));
+    std::vector<midsx_grid_spec> grids(static_cast<size_t>(n_grids));
+    for (int k = 0; k < n_grids; ++k) {
+        VoxelGrid& g = comp_domain_.getVoxelGridN(k);
+        midsx_grid_spec& gs = grids[size_t(k)];
+        std::memset(&gs, 0, sizeof(gs));
+        const Vec3 org = comp_domain_.getVoxelGridOriginN(k), sp = g.getSpacing();
+        const VoxelIndex dims = g.getDimVox();
+        for (int i = 0; i < 3; ++i) {
+            gs.origin[i] = org(i);
+            gs.spacing[i] = sp(i);
+            gs.dims[i] = dims[size_t(i)];
+        }
+        ids[size_t(k)] = g.getMaterialIdArray();
+        gs.ids = ids[size_t(k)].data();
     }
-    geom.background_id = comp_domain_.background_voxel.materialID;
-    std::vector<uint8_t> ids = g.getMaterialIdArray();
-    check(midsx_gpu_phantom_create(d->tables, &geom, ids.data(), &d->phantom), "midsx_gpu_phantom_create");
+    const Vec3 dom = comp_domain_.getDimSpace();
+    const double domain[3] = {dom(0), dom(1), dom(2)};
+    check(midsx_gpu_phantom_create_grids(d->tables, domain, comp_domain_.background_voxel.materialID, grids.data(),
+                                         n_grids, &d->phantom),
+          "midsx_gpu_phantom_create_grids");
     std::vector<midsx_tally_spec> specs;
     for (auto& t : surface_tallies_) specs.push_back(t->describe());
     for (auto& t : volume_tallies_) specs.push_back(t->describe());
@@ -140,7 +149,8 @@ double PhysicsEngine::run(PhotonSource& source, uint64_t n_photons) {
         }
         ++k;
     }
-    size_t nv = comp_domain_.getVoxelGridN(0).getNumberOfVoxels();
+    size_t nv = 0;
+    for (int k = 0; k < comp_domain_.getNumVoxelGrids(); ++k) nv += comp_domain_.getVoxelGridN(k).getNumberOfVoxels();
     dose_sum_.resize(nv);
     dose_sumsq_.resize(nv);
     dose_count_.resize(nv);
@@ -172,11 +182,16 @@ std::vector<BinnedRectangularSurfaceTally*> PhysicsEngine::getBinnedSurfaceTalli
 
 void PhysicsEngine::addVoxelDataToComputationalDomain() {
     if (!dose_pending_) return;
-    std::vector<Voxel>& vox = comp_domain_.getVoxelGridN(0).voxels();
-    for (size_t i = 0; i < vox.size(); ++i) {
-        VectorValue v;
-        v.addSummary(dose_count_[i], dose_sum_[i], dose_sumsq_[i]);
-        vox[i].dose = v;
+    // the device numbers voxels grid after grid
+    size_t off = 0;
+    for (int k = 0; k < comp_domain_.getNumVoxelGrids(); ++k) {
+        std::vector<Voxel>& vox = comp_domain_.getVoxelGridN(k).voxels();
+        for (size_t i = 0; i < vox.size(); ++i) {
+            VectorValue v;
+            v.addSummary(dose_count_[off + i], dose_sum_[off + i], dose_sumsq_[off + i]);
+            vox[i].dose = v;
+        }
+        off += vox.size();
     }
     dose_pending_ = false;
 }

@@ -118,6 +118,8 @@ struct Geo {
     V3<R> dom, org, ext, spc, ispc;
     int nx, ny, nz, bg;
     const uint8_t* ids;
+    int n_grids;           // grids of the domain; the first is held above
+    const DevGrid* extra;  // the others, in first-hit order
 };
 
 template <typename R>
@@ -133,7 +135,79 @@ __device__ Geo<R> make_geo(const DevGeom& G) {
     g.nz = G.dims[2];
     g.bg = G.background;
     g.ids = G.ids;
+    g.n_grids = G.n_grids;
+    g.extra = G.extra;
     return g;
+}
+
+// ComputationalDomain::getVoxel (computational_domain.cpp:23-31) for a point of the domain:
+// the first grid whose closed box holds the point gives the voxel - vox is its number in the
+// phantom (grid after grid), mat its material - else the background (vox = -1).  Inside a grid
+// the index is trunc(offset / spacing) (VoxelGrid::getVoxelIndex, voxel_grid.cpp:55-59); the
+// FP32 form multiplies by the reciprocal spacing, the FP64 form divides as the reference does.
+// An index equal to the grid size (the point on the far face, where the reference's
+// vector::at would throw) is clamped and counted.
+template <typename R, bool MX>
+__device__ __forceinline__ void locate(const Geo<R>& g, const V3<R>& pos, int& vox, int& mat, uint32_t& fetches,
+                                       unsigned long long* st) {
+    vox = -1;
+    mat = g.bg;
+    const V3<R> q = {pos.x - g.org.x, pos.y - g.org.y, pos.z - g.org.z};
+    if (q.x >= R(0) && q.x <= g.ext.x && q.y >= R(0) && q.y <= g.ext.y && q.z >= R(0) && q.z <= g.ext.z) {
+        int ix, iy, iz;
+        if constexpr (MX) {
+            ix = int(q.x * g.ispc.x);
+            iy = int(q.y * g.ispc.y);
+            iz = int(q.z * g.ispc.z);
+        } else {
+            ix = int(q.x / g.spc.x);
+            iy = int(q.y / g.spc.y);
+            iz = int(q.z / g.spc.z);
+        }
+        if (ix >= g.nx || iy >= g.ny || iz >= g.nz) {
+            stat_add(st, kStEdge, 1);
+            ix = min(ix, g.nx - 1);
+            iy = min(iy, g.ny - 1);
+            iz = min(iz, g.nz - 1);
+        }
+        vox = ix + iy * g.nx + iz * g.nx * g.ny;
+        mat = __ldg(g.ids + vox);
+        ++fetches;
+        return;
+    }
+    for (int k = 0; k + 1 < g.n_grids; ++k) {
+        const DevGrid& G = g.extra[k];
+        V3<R> o, e;
+        if constexpr (MX) {
+            o = {G.f_origin[0], G.f_origin[1], G.f_origin[2]};
+            e = {G.f_ext[0], G.f_ext[1], G.f_ext[2]};
+        } else {
+            o = {G.origin[0], G.origin[1], G.origin[2]};
+            e = {G.ext[0], G.ext[1], G.ext[2]};
+        }
+        const V3<R> r = {pos.x - o.x, pos.y - o.y, pos.z - o.z};
+        if (!(r.x >= R(0) && r.x <= e.x && r.y >= R(0) && r.y <= e.y && r.z >= R(0) && r.z <= e.z)) continue;
+        int ix, iy, iz;
+        if constexpr (MX) {
+            ix = int(r.x * G.f_ispc[0]);
+            iy = int(r.y * G.f_ispc[1]);
+            iz = int(r.z * G.f_ispc[2]);
+        } else {
+            ix = int(r.x / G.spacing[0]);
+            iy = int(r.y / G.spacing[1]);
+            iz = int(r.z / G.spacing[2]);
+        }
+        if (ix >= G.dims[0] || iy >= G.dims[1] || iz >= G.dims[2]) {
+            stat_add(st, kStEdge, 1);
+            ix = min(ix, G.dims[0] - 1);
+            iy = min(iy, G.dims[1] - 1);
+            iz = min(iz, G.dims[2] - 1);
+        }
+        vox = G.offset + ix + iy * G.dims[0] + iz * G.dims[0] * G.dims[1];
+        mat = __ldg(g.ids + vox);
+        ++fetches;
+        return;
+    }
 }
 
 // Shared-memory bytes of a launch: per-job counters, the batch's prefix table and geometry,
@@ -227,33 +301,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
                     stat_add(st, kStEscE, fx_stat(E));
                     finish = true;
                 } else {
-                    const V3<R> q = {pos.x - g.org.x, pos.y - g.org.y, pos.z - g.org.z};
-                    vox = -1;
-                    mat = g.bg;
-                    if (q.x >= R(0) && q.x <= g.ext.x && q.y >= R(0) && q.y <= g.ext.y && q.z >= R(0) &&
-                        q.z <= g.ext.z) {
-                        int ix, iy, iz;
-                        if constexpr (MX) {
-                            // the FP32 form multiplies by the reciprocal voxel size; the FP64
-                            // form divides exactly as the reference does
-                            ix = int(q.x * g.ispc.x);
-                            iy = int(q.y * g.ispc.y);
-                            iz = int(q.z * g.ispc.z);
-                        } else {
-                            ix = int(q.x / g.spc.x);
-                            iy = int(q.y / g.spc.y);
-                            iz = int(q.z / g.spc.z);
-                        }
-                        if (ix >= g.nx || iy >= g.ny || iz >= g.nz) {
-                            stat_add(st, kStEdge, 1);  // the reference's vector::at would throw here
-                            ix = min(ix, g.nx - 1);
-                            iy = min(iy, g.ny - 1);
-                            iz = min(iz, g.nz - 1);
-                        }
-                        vox = ix + iy * g.nx + iz * g.nx * g.ny;
-                        mat = __ldg(g.ids + vox);
-                        ++fetches;
-                    }
+                    locate<R, MX>(g, pos, vox, mat, fetches, st);
                     if (to_uniform(w2, R(0)) < thr[mat * stride]) {
                         if (ntal) {
                             const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;

@@ -50,14 +50,20 @@ __host__ __device__ inline size_t pool_head_bytes(int n_jobs, bool multi) {
 }
 
 // Shared-memory bytes of a pool launch: per-job counters, batch prefix and geometry, the
-// slots, then each warp's ready and event lists (one byte per entry).
+// slots, each warp's 32-word scratch for aggregated tallies, then each warp's ready and
+// event lists (one byte per entry).
 template <typename R>
-__host__ __device__ inline size_t pool_smem(int n_jobs, bool multi, int n_materials, int block) {
+__host__ __device__ inline size_t pool_scratch_offset(int n_jobs, bool multi, int n_materials, int block) {
     const size_t ns = size_t(block / 32) * kPoolSlots;
     size_t b = pool_head_bytes<R>(n_jobs, multi);
     b += ns * (kPoolRealWords * sizeof(R) + kPoolIntWords * 4 + 2 * size_t(n_materials) * sizeof(R));
-    b = (b + 15) & ~size_t(15);
-    return b + size_t(block / 32) * 2 * kPoolSlots;
+    return (b + 15) & ~size_t(15);
+}
+
+template <typename R>
+__host__ __device__ inline size_t pool_smem(int n_jobs, bool multi, int n_materials, int block) {
+    return pool_scratch_offset<R>(n_jobs, multi, n_materials, block) + size_t(block / 32) * 32 * 8 +
+           size_t(block / 32) * 2 * kPoolSlots;
 }
 
 template <typename R, bool MULTI>
@@ -92,6 +98,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
         }
     }
     uint8_t* stacks = smem_raw + pool_smem<R>(njobs, MULTI, M, int(blockDim.x)) - size_t(nw) * 2 * kPoolSlots;
+    unsigned long long* scratch = reinterpret_cast<unsigned long long*>(
+                                      smem_raw + pool_scratch_offset<R>(njobs, MULTI, M, int(blockDim.x))) +
+                                  (threadIdx.x >> 5) * 32;
     for (int i = threadIdx.x; i < njobs * kStCount; i += blockDim.x) s_stats[i] = 0;
     if (MULTI) {
         for (int i = threadIdx.x; i <= njobs; i += blockDim.x) s_prefix[i] = P.prefix[i];
@@ -209,11 +218,11 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
         }
         if (__ballot_sync(FULL, cur >= 0) == 0u && rdy_top == 0 && ev_top == 0) break;
         uint32_t park = kKindFlight;
+        bool segment = false;  // the step's segment goes to the tallies (escape or delta step)
         if (cur >= 0) {
             // one Woodcock step: getFreePath, move, domain test, voxel fetch, isDeltaScatter
             const Geo<R>& g = MULTI ? s_geo[job] : g0;
             unsigned long long* st = s_stats + job * kStCount;
-            bool segment = false;  // the step's segment goes to the tallies (escape or delta step)
             if (steps >= uint32_t(P.max_steps)) {
                 stat_add(st, kStStepCap, 1);
                 park = kKindStart;
@@ -233,45 +242,23 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                     segment = true;
                     park = kKindStart;
                 } else {
-                    const V3<R> q = {pos.x - g.org.x, pos.y - g.org.y, pos.z - g.org.z};
-                    vox = -1;
-                    mat = g.bg;
-                    if (q.x >= R(0) && q.x <= g.ext.x && q.y >= R(0) && q.y <= g.ext.y && q.z >= R(0) &&
-                        q.z <= g.ext.z) {
-                        int ix, iy, iz;
-                        if constexpr (MX) {
-                            ix = int(q.x * g.ispc.x);
-                            iy = int(q.y * g.ispc.y);
-                            iz = int(q.z * g.ispc.z);
-                        } else {
-                            ix = int(q.x / g.spc.x);
-                            iy = int(q.y / g.spc.y);
-                            iz = int(q.z / g.spc.z);
-                        }
-                        if (ix >= g.nx || iy >= g.ny || iz >= g.nz) {
-                            stat_add(st, kStEdge, 1);  // the reference's vector::at would throw here
-                            ix = min(ix, g.nx - 1);
-                            iy = min(iy, g.ny - 1);
-                            iz = min(iz, g.nz - 1);
-                        }
-                        vox = ix + iy * g.nx + iz * g.nx * g.ny;
-                        mat = __ldg(g.ids + vox);
-                        ++fetches;
-                    }
+                    locate<R, MX>(g, pos, vox, mat, fetches, st);
                     if (to_uniform(w2, R(0)) < S.thr[mat * ns + cur])
                         segment = true;
                     else
                         park = kKindCollide;  // a real collision
                 }
             }
-            // surface and volume tallies see every step that does not interact, the last
-            // (escaping) one included (physics_engine.cpp:48-49)
-            if (segment && ntal) {
-                const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
-                score_tallies<R, MX>(tal, ntal, p0, dir, s, E, scatter_class(n_coh, n_incoh), 0, false, R(0), words);
-            }
-            if (park == kKindStart) end_history();
         }
+        // surface and volume tallies see every step that does not interact, the last (escaping)
+        // one included (physics_engine.cpp:48-49).  Scored per lane: nearly every step runs
+        // this and almost none touches a tally, so the warp-collective form (used for the
+        // collisions below) measured 3 % slower on the cone-beam dose workload and 29 % slower
+        // on the radiography workload.
+        if (segment && ntal > 0)
+            score_tallies<R, MX>(MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, dir, s, E,
+                                 scatter_class(n_coh, n_incoh), 0, false, R(0), words);
+        if (cur >= 0 && park == kKindStart) end_history();
         // photons that need an event go to the event list
         {
             const bool parks = park != kKindFlight;
@@ -296,7 +283,10 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
         const int n_ev = min(ev_top, 32);
         int sl = int(lane) < n_ev ? sbase + evq[ev_top - 1 - int(lane)] : -1;
         ev_top -= n_ev;
-        bool need_start = false, need_refresh = false;
+        bool need_start = false, need_refresh = false, scored = false, ended = false;
+        R dep = R(0), E0 = R(0);
+        V3<R> d0 = {R(0), R(0), R(0)};
+        int cls0 = 0;
         if (sl >= 0) {
             load_event(sl);
             if (kind != kKindCollide) {
@@ -310,10 +300,10 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                 R p_coh, p_incoh;
                 interaction_probs<R>(P.T, Mt, E, mu_tot, p_coh, p_incoh);
                 const R u3 = uniform<R>(rng);
-                const int cls0 = scatter_class(n_coh, n_incoh);
-                const R E0 = E;
-                const V3<R> d0 = dir;
-                R dep = R(0), mu_s = R(1);
+                cls0 = scatter_class(n_coh, n_incoh);
+                E0 = E;
+                d0 = dir;
+                R mu_s = R(1);
                 bool energy_changed = false, failed = false, scattered = false;
                 if (u3 < p_coh) {
                     // CoherentScattering::interact
@@ -358,23 +348,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                 if (failed) {
                     finish = true;
                 } else {
-                    if (ntal) {
-                        const DevTally* tal = MULTI ? P.jobs[job].tallies : P.job0.tallies;
-                        score_tallies<R, MX>(tal, ntal, p0, d0, s, E0, cls0, scatter_class(n_coh, n_incoh), true, dep,
-                                             words);
-                    }
-                    if (dep != R(0)) {
-                        if (vox >= 0) {
-                            stat_add(st, kStDepGrid, fx_stat(dep));
-                            const DevJob& J = MULTI ? P.jobs[job] : P.job0;
-                            if (J.dose_stride) {
-                                score_dose<R, MX>(J.dose, J.dose_stride, vox, dep);
-                                ++words;
-                            }
-                        } else {
-                            stat_add(st, kStDepBg, fx_stat(dep));
-                        }
-                    }
+                    scored = true;  // tallies and dose below, with the whole warp
+                    if (dep != R(0)) stat_add(st, vox >= 0 ? kStDepGrid : kStDepBg, fx_stat(dep));
                     if (!finish) {
                         if (!(fabs_(dir.x) <= R(2) && fabs_(dir.y) <= R(2) && fabs_(dir.z) <= R(2))) {
                             // a NaN direction (RITA rows below ~400 eV are NaN, as in the
@@ -387,11 +362,23 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                         }
                     }
                 }
-                if (finish) {
-                    end_history();
-                    need_start = true;
-                }
+                ended = finish;
             }
+        }
+        // the collisions' tallies and voxel dose, aggregated over the warp
+        if (__any_sync(FULL, scored && ntal > 0))
+            score_tallies_warp<R, MX>(scored && ntal > 0, MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, d0,
+                                      s, E0, cls0, scatter_class(n_coh, n_incoh), true, dep, words, scratch);
+        {
+            const DevJob& J = MULTI ? P.jobs[job] : P.job0;
+            const bool dosed = scored && dep != R(0) && vox >= 0 && J.dose_stride != 0;
+            if (dosed) ++words;
+            warp_record<R, MX>(dosed ? kRecDose : kRecNone, dosed ? J.dose + size_t(vox) * J.dose_stride : nullptr,
+                               J.dose_stride, dep, R(0), scratch);
+        }
+        if (ended) {
+            end_history();
+            need_start = true;
         }
         // new histories: one atomic per warp hands out the lanes' history indices
         const unsigned nm = __ballot_sync(FULL, need_start);

@@ -61,11 +61,23 @@ struct DevSource {
 };
 constexpr int kCdfGuide = 256;  // a power of two: k / kCdfGuide and u * kCdfGuide are exact
 
+// Voxel grids after the first of a domain (ComputationalDomain::voxel_grids_[1..]).  The
+// FP32 copies are what the mixed form computes with: float origin and extent, and the
+// reciprocal of the float spacing, as make_geo derives them for the first grid.
+struct DevGrid {
+    double origin[3], spacing[3], ext[3];
+    float f_origin[3], f_ext[3], f_ispc[3];
+    int dims[3];
+    int offset;  // number of the grid's first voxel in the phantom (ids and dose tally)
+};
+
 struct DevGeom {
     double domain[3], origin[3], spacing[3], ext[3];
     int dims[3];
     int background;
-    const uint8_t* ids;
+    const uint8_t* ids;     // every grid's dense material indices, grid after grid
+    int n_grids;            // grids of the domain (1 = the first alone)
+    const DevGrid* extra;   // n_grids - 1 further grids (device memory), in first-hit order
 };
 
 // One simulation: geometry, source, tallies and its history range [first, first + n) of its
@@ -334,6 +346,7 @@ __device__ __forceinline__ void sample_source(const DevSource& S, HistoryRng& rn
 
 // -------------------------------------------------------------------- the kernel ---
 #include "kernel_body.cuh"
+#include "tally_warp.cuh"
 #include "kernel_pool.cuh"
 // ------------------------------------------------------------- diagnostics kernels ---
 template <typename R>
@@ -439,7 +452,8 @@ struct midsx_gpu_tables {
 struct midsx_gpu_phantom {
     DevGeom G;
     uint8_t* ids = nullptr;
-    size_t n_voxels = 0;
+    size_t n_voxels = 0;                       // all grids
+    DevGrid* extra = nullptr;                  // grids after the first (device)
     const midsx_gpu_tables* tables = nullptr;  // the tables its dense material indices refer to
 };
 
@@ -674,74 +688,154 @@ extern "C" midsx_status midsx_gpu_tables_destroy(midsx_tables_h t) {
     return MIDSX_OK;
 }
 
-extern "C" midsx_status midsx_gpu_phantom_create(midsx_tables_h tables, const midsx_geometry_spec* g,
-                                                 const uint8_t* ids, midsx_phantom_h* out) {
-    if (!tables || !g || !ids || !out) return MIDSX_INVALID_ARG;
-    for (int i = 0; i < 3; ++i) {
-        if (g->dims[i] < 1 || !(g->spacing[i] > 0) || !(g->domain[i] > 0)) {
-            set_last_error("midsx_gpu_phantom_create: bad geometry");
+namespace {
+
+// Uploads the grids' voxel ids (concatenated, grid after grid), remaps them to the tables'
+// dense material indices and fills the domain description.
+midsx_status phantom_create_impl(midsx_tables_h tables, const double* domain, int32_t background_id,
+                                 const midsx_grid_spec* grids, int n_grids, midsx_phantom_h* out) {
+    if (!tables || !domain || !grids || !out || n_grids < 1 || n_grids > MIDSX_MAX_GRIDS) {
+        set_last_error("midsx_gpu_phantom_create: invalid argument (1..16 grids)");
+        return MIDSX_INVALID_ARG;
+    }
+    size_t total = 0;
+    for (int k = 0; k < n_grids; ++k) {
+        const midsx_grid_spec& g = grids[k];
+        for (int i = 0; i < 3; ++i) {
+            if (g.dims[i] < 1 || !(g.spacing[i] > 0) || !(domain[i] > 0)) {
+                set_last_error("midsx_gpu_phantom_create: bad geometry");
+                return MIDSX_INVALID_ARG;
+            }
+        }
+        if (!g.ids) {
+            set_last_error("midsx_gpu_phantom_create: missing voxel ids");
             return MIDSX_INVALID_ARG;
         }
+        total += size_t(g.dims[0]) * g.dims[1] * g.dims[2];
+    }
+    if (total > size_t(0x7fffffff)) {
+        set_last_error("midsx_gpu_phantom_create: more than 2^31 - 1 voxels");
+        return MIDSX_INVALID_ARG;
     }
     uint8_t lut[256];
     std::memset(lut, 0xFF, sizeof(lut));
     int bg = -1;
     for (int m = 0; m < tables->T.n_materials; ++m) {
         lut[tables->ids[m] & 0xFF] = uint8_t(m);
-        if (tables->ids[m] == g->background_id) bg = m;
+        if (tables->ids[m] == background_id) bg = m;
     }
     if (bg < 0) {
         set_last_error("background material not in tables");
         return MIDSX_NOT_FOUND;
     }
     auto* p = new midsx_gpu_phantom();
-    p->n_voxels = size_t(g->dims[0]) * g->dims[1] * g->dims[2];
+    p->n_voxels = total;
     uint8_t *raw = nullptr, *dlut = nullptr;
     int* bad = nullptr;
-    if (!cuda_ok(cudaMalloc(&p->ids, p->n_voxels), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&raw, p->n_voxels), "cudaMalloc") || !cuda_ok(cudaMalloc(&dlut, 256), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&bad, sizeof(int)), "cudaMalloc")) {
-        cudaFree(p->ids);
+    auto release = [&]() {
         cudaFree(raw);
         cudaFree(dlut);
         cudaFree(bad);
-        delete p;
+    };
+    if (!cuda_ok(cudaMalloc(&p->ids, total), "cudaMalloc") || !cuda_ok(cudaMalloc(&raw, total), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&dlut, 256), "cudaMalloc") || !cuda_ok(cudaMalloc(&bad, sizeof(int)), "cudaMalloc") ||
+        (n_grids > 1 && !cuda_ok(cudaMalloc(&p->extra, sizeof(DevGrid) * (n_grids - 1)), "cudaMalloc"))) {
+        release();
+        midsx_gpu_phantom_destroy(p);
         return MIDSX_OOM;
     }
-    CUDA_TRY(cudaMemcpy(raw, ids, p->n_voxels, cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(dlut, lut, 256, cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemset(bad, 0, sizeof(int)));
-    remap_kernel<<<tables->sm_count * 8, 256>>>(raw, p->ids, dlut, p->n_voxels, bad);
-    CUDA_TRY(cudaGetLastError());
+    std::vector<DevGrid> extra;
+    size_t off = 0;
+    for (int k = 0; k < n_grids; ++k) {
+        const midsx_grid_spec& g = grids[k];
+        const size_t n = size_t(g.dims[0]) * g.dims[1] * g.dims[2];
+        if (!cuda_ok(cudaMemcpy(raw + off, g.ids, n, cudaMemcpyHostToDevice), "cudaMemcpy")) {
+            release();
+            midsx_gpu_phantom_destroy(p);
+            return MIDSX_CUDA_ERROR;
+        }
+        if (k > 0) {
+            DevGrid d;
+            std::memset(&d, 0, sizeof(d));
+            for (int i = 0; i < 3; ++i) {
+                d.origin[i] = g.origin[i];
+                d.spacing[i] = g.spacing[i];
+                d.ext[i] = double(g.dims[i]) * g.spacing[i];  // VoxelGrid::setDimSpace
+                d.dims[i] = g.dims[i];
+                d.f_origin[i] = float(d.origin[i]);
+                d.f_ext[i] = float(d.ext[i]);
+                d.f_ispc[i] = 1.0f / float(d.spacing[i]);
+            }
+            d.offset = int(off);
+            extra.push_back(d);
+        }
+        off += n;
+    }
+    bool good = cuda_ok(cudaMemcpy(dlut, lut, 256, cudaMemcpyHostToDevice), "cudaMemcpy") &&
+                cuda_ok(cudaMemset(bad, 0, sizeof(int)), "cudaMemset") &&
+                (extra.empty() || cuda_ok(cudaMemcpy(p->extra, extra.data(), sizeof(DevGrid) * extra.size(),
+                                                     cudaMemcpyHostToDevice),
+                                          "cudaMemcpy"));
     int hbad = 0;
-    CUDA_TRY(cudaMemcpy(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost));
-    cudaFree(raw);
-    cudaFree(dlut);
-    cudaFree(bad);
+    if (good) {
+        remap_kernel<<<tables->sm_count * 8, 256>>>(raw, p->ids, dlut, total, bad);
+        good = cuda_ok(cudaGetLastError(), "remap_kernel") &&
+               cuda_ok(cudaMemcpy(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
+    }
+    release();
+    if (!good) {
+        midsx_gpu_phantom_destroy(p);
+        return MIDSX_CUDA_ERROR;
+    }
     if (hbad) {
-        cudaFree(p->ids);
-        delete p;
+        midsx_gpu_phantom_destroy(p);
         set_last_error("voxel material id not among the tables' materials");
         return MIDSX_NOT_FOUND;
     }
     DevGeom& G = p->G;
+    const midsx_grid_spec& g0 = grids[0];
     for (int i = 0; i < 3; ++i) {
-        G.domain[i] = g->domain[i];
-        G.origin[i] = g->origin[i];
-        G.spacing[i] = g->spacing[i];
-        G.dims[i] = g->dims[i];
-        G.ext[i] = double(g->dims[i]) * g->spacing[i];  // VoxelGrid::setDimSpace
+        G.domain[i] = domain[i];
+        G.origin[i] = g0.origin[i];
+        G.spacing[i] = g0.spacing[i];
+        G.dims[i] = g0.dims[i];
+        G.ext[i] = double(g0.dims[i]) * g0.spacing[i];  // VoxelGrid::setDimSpace
     }
     G.background = bg;
     G.ids = p->ids;
+    G.n_grids = n_grids;
+    G.extra = p->extra;
     p->tables = tables;
     *out = p;
     return MIDSX_OK;
 }
 
+}  // namespace
+
+extern "C" midsx_status midsx_gpu_phantom_create(midsx_tables_h tables, const midsx_geometry_spec* g,
+                                                 const uint8_t* ids, midsx_phantom_h* out) {
+    if (!tables || !g || !ids || !out) return MIDSX_INVALID_ARG;
+    midsx_grid_spec one;
+    std::memset(&one, 0, sizeof(one));
+    for (int i = 0; i < 3; ++i) {
+        one.spacing[i] = g->spacing[i];
+        one.origin[i] = g->origin[i];
+        one.dims[i] = g->dims[i];
+    }
+    one.ids = ids;
+    return phantom_create_impl(tables, g->domain, g->background_id, &one, 1, out);
+}
+
+extern "C" midsx_status midsx_gpu_phantom_create_grids(midsx_tables_h tables, const double* domain,
+                                                       int32_t background_id, const midsx_grid_spec* grids,
+                                                       int32_t n_grids, midsx_phantom_h* out) {
+    return phantom_create_impl(tables, domain, background_id, grids, n_grids, out);
+}
+
 extern "C" midsx_status midsx_gpu_phantom_destroy(midsx_phantom_h p) {
     if (!p) return MIDSX_INVALID_ARG;
     cudaFree(p->ids);
+    cudaFree(p->extra);
     delete p;
     return MIDSX_OK;
 }

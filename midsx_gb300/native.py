@@ -61,6 +61,10 @@ class GeometrySpec(C.Structure):
                 ("background_id", C.c_int32)]
 
 
+class GridSpec(C.Structure):
+    _fields_ = [("spacing", D3), ("origin", D3), ("dims", I3), ("reserved", C.c_int32), ("ids", C.c_void_p)]
+
+
 class SourceSpec(C.Structure):
     _fields_ = [("position", D3), ("direction_kind", C.c_int32), ("spectrum_kind", C.c_int32),
                 ("a", D3), ("b", D3), ("c", D3), ("radius", C.c_double),
@@ -150,6 +154,8 @@ _SIGNATURES = {
     "midsx_gpu_tables_destroy": (C.c_int, [VP]),
     "midsx_gpu_phantom_create": (C.c_int, [VP, C.POINTER(GeometrySpec), C.c_void_p, C.POINTER(VP)]),
     "midsx_gpu_phantom_destroy": (C.c_int, [VP]),
+    "midsx_gpu_phantom_create_grids": (C.c_int, [VP, C.POINTER(C.c_double), C.c_int32, C.POINTER(GridSpec), C.c_int32,
+                                                 C.POINTER(VP)]),
     "midsx_gpu_source_create": (C.c_int, [C.POINTER(SourceSpec), C.POINTER(VP)]),
     "midsx_gpu_source_destroy": (C.c_int, [VP]),
     "midsx_gpu_tallies_create": (C.c_int, [VP, C.POINTER(TallySpec), C.c_int32, C.c_int32, C.POINTER(VP)]),

@@ -42,6 +42,11 @@ def load():
                                    C.POINTER(N.SourceSpec), C.POINTER(N.TallySpec), C.c_int, C.c_uint64,
                                    C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int,
                                    C.POINTER(OracleResult)]
+        lib.oracle_run_grids.restype = C.c_int
+        lib.oracle_run_grids.argtypes = [C.POINTER(N.TableBlob), C.POINTER(C.c_double), C.c_int,
+                                         C.POINTER(N.GridSpec), C.c_int, C.POINTER(N.SourceSpec),
+                                         C.POINTER(N.TallySpec), C.c_int, C.c_uint64, C.c_uint64, C.c_uint64,
+                                         C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(OracleResult)]
         lib.oracle_sample.restype = C.c_int
         lib.oracle_sample.argtypes = [C.POINTER(N.TableBlob), C.c_int, C.c_int, C.c_double, C.c_uint64,
                                       C.c_uint64, C.c_int64, C.c_int, PD, PD]
@@ -55,13 +60,28 @@ def load():
 
 
 def run(blob, domain, spacing, origin, ids, background_id, source, specs=(), n=1000, seed=1, first=0,
-        rng=RNG_PHILOX, threads=0, max_steps=0, max_trials=0, dose=True, history=False):
+        rng=RNG_PHILOX, threads=0, max_steps=0, max_trials=0, dose=True, history=False, grids=None):
     """blob: midsx_gb300.TableBlob; ids shaped (nz, ny, nx); source: dict(position, direction,
-    energy|spectrum) as for midsx_gb300.source_spec; specs: tally dicts."""
+    energy|spectrum) as for midsx_gb300.source_spec; specs: tally dicts.  grids: optional list
+    of (ids, spacing, origin) for a domain of several grids (then spacing, origin and ids are
+    ignored and dose arrays come as one list entry per grid)."""
     lib = load()
-    ids = np.ascontiguousarray(ids, dtype=np.uint8)
-    nz, ny, nx = ids.shape
-    g = geometry_spec(domain, spacing, origin, (nx, ny, nz), background_id)
+    shapes = None
+    if grids is not None:
+        garr = (N.GridSpec * len(grids))()
+        gkeep = []
+        for k, (gids, gsp, gor) in enumerate(grids):
+            gids = np.ascontiguousarray(gids, dtype=np.uint8)
+            gz, gy, gx = gids.shape
+            garr[k].spacing, garr[k].origin, garr[k].dims = N.vec3(gsp), N.vec3(gor), N.I3(gx, gy, gz)
+            garr[k].ids = gids.ctypes.data
+            gkeep.append(gids)
+        shapes = [a.shape for a in gkeep]
+        ids = np.concatenate([a.ravel() for a in gkeep])
+    else:
+        ids = np.ascontiguousarray(ids, dtype=np.uint8)
+        nz, ny, nx = ids.shape
+        g = geometry_spec(domain, spacing, origin, (nx, ny, nz), background_id)
     s = source_spec(**source)
     arr = tally_specs(list(specs))
     res = OracleResult()
@@ -82,14 +102,32 @@ def run(blob, domain, spacing, origin, ids, background_id, source, specs=(), n=1
     if history:
         keep["history_deposit"] = np.zeros(int(n))
         res.history_deposit = N.dptr(keep["history_deposit"])
-    rc = lib.oracle_run(blob.ptr, C.byref(g), ids.ctypes.data, C.byref(s), arr, len(specs), int(seed), int(first),
-                        int(n), int(rng), int(threads), int(max_steps), int(max_trials), C.byref(res))
+    if grids is not None:
+        dom = (C.c_double * 3)(*[float(x) for x in domain])
+        rc = lib.oracle_run_grids(blob.ptr, dom, int(background_id), garr, len(grids), C.byref(s), arr, len(specs),
+                                  int(seed), int(first), int(n), int(rng), int(threads), int(max_steps),
+                                  int(max_trials), C.byref(res))
+    else:
+        rc = lib.oracle_run(blob.ptr, C.byref(g), ids.ctypes.data, C.byref(s), arr, len(specs), int(seed),
+                            int(first), int(n), int(rng), int(threads), int(max_steps), int(max_trials),
+                            C.byref(res))
     if rc != 0:
         raise RuntimeError("oracle_run failed with code %d" % rc)
     out = {"stats": res.stats.as_dict(), "run_time": res.run_time}
+
+    def shaped(a):
+        if shapes is None:
+            return a.reshape(ids.shape)
+        parts, off = [], 0
+        for sh in shapes:
+            k = int(np.prod(sh))
+            parts.append(a[off:off + k].reshape(sh))
+            off += k
+        return parts
+
     if dose:
-        out["dose"] = {"sum": keep["dose_sum"].reshape(ids.shape), "sumsq": keep["dose_sumsq"].reshape(ids.shape),
-                       "count": keep["dose_count"].reshape(ids.shape)}
+        out["dose"] = {"sum": shaped(keep["dose_sum"]), "sumsq": shaped(keep["dose_sumsq"]),
+                       "count": shaped(keep["dose_count"])}
     out["scalar"] = [keep["scalar"][i * N.SCALAR_SLOTS:(i + 1) * N.SCALAR_SLOTS] for i in range(n_scalar)]
     binned, off = [], 0
     for d in specs:

@@ -452,27 +452,39 @@ struct PhotonSource {
 };
 
 // ---------------------------------------------------------------------- geometry ------
-struct ComputationalDomain {
-    Vec3 dim_space, origin, spacing, grid_dim;
+// VoxelGrid at an origin: extent dims * spacing (VoxelGrid::setDimSpace), first voxel number
+// `offset` in the domain's grid-after-grid numbering.
+struct Grid {
+    Vec3 origin, spacing, grid_dim;
     int dims[3] = {0, 0, 0};
-    int background = 0;  // dense material index
-    std::vector<uint8_t> ids;  // dense material index per voxel
+    long offset = 0;
+};
+
+struct ComputationalDomain {
+    Vec3 dim_space;
+    std::vector<Grid> grids;   // voxel_grids_, searched in order
+    int background = 0;        // dense material index
+    std::vector<uint8_t> ids;  // dense material index per voxel, grid after grid
 
     bool isInComputationalDomain(const Vec3& p) const {
         return p.x >= 0 && p.x <= dim_space.x && p.y >= 0 && p.y <= dim_space.y && p.z >= 0 && p.z <= dim_space.z;
     }
-    // returns the voxel number, or -1 for the background voxel
+    // the first grid containing p (withinGrid, inclusive bounds) gives the voxel: returns its
+    // number, or -1 for the background voxel
     long getVoxel(const Vec3& p, int& mat) const {
-        Vec3 q = p - origin;
-        if (q.x >= 0 && q.y >= 0 && q.z >= 0 && q.x <= grid_dim.x && q.y <= grid_dim.y && q.z <= grid_dim.z) {
-            int i = int(q.x / spacing.x), j = int(q.y / spacing.y), k = int(q.z / spacing.z);
-            if (i >= dims[0] || j >= dims[1] || k >= dims[2]) {
+        for (const Grid& g : grids) {
+            Vec3 q = p - g.origin;
+            if (!(q.x >= 0 && q.y >= 0 && q.z >= 0 && q.x <= g.grid_dim.x && q.y <= g.grid_dim.y &&
+                  q.z <= g.grid_dim.z))
+                continue;
+            int i = int(q.x / g.spacing.x), j = int(q.y / g.spacing.y), k = int(q.z / g.spacing.z);
+            if (i >= g.dims[0] || j >= g.dims[1] || k >= g.dims[2]) {
                 tl_cnt->edge++;
-                i = std::min(i, dims[0] - 1);
-                j = std::min(j, dims[1] - 1);
-                k = std::min(k, dims[2] - 1);
+                i = std::min(i, g.dims[0] - 1);
+                j = std::min(j, g.dims[1] - 1);
+                k = std::min(k, g.dims[2] - 1);
             }
-            long n = long(i) + long(j) * dims[0] + long(k) * dims[0] * dims[1];
+            long n = g.offset + long(i) + long(j) * g.dims[0] + long(k) * g.dims[0] * g.dims[1];
             mat = ids[size_t(n)];
             tl_cnt->fetches++;
             return n;
@@ -720,32 +732,97 @@ typedef struct oracle_result {
     double run_time;        /* seconds in the history loop (the reference's run_time) */
 } oracle_result;
 
+}  // extern "C"
+
+namespace {
+
+// The history loop over an assembled domain; nvox = voxels of all grids.
+int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size_t nvox, const midsx_source_spec* src,
+               const midsx_tally_spec* specs, int n_specs, uint64_t seed, uint64_t first, uint64_t n, int rng_mode,
+               int n_threads, int max_steps, int max_trials, oracle_result* out);
+
+// Domain of `n_grids` grids with MIDSX material ids, remapped to the tables' dense indices.
+int build_domain(const midsx_table_blob* blob, const double* domain, int background_id, const midsx_grid_spec* grids,
+                 int n_grids, ref::ComputationalDomain& dom, size_t& nvox) {
+    using namespace ref;
+    dom.dim_space = Vec3(domain[0], domain[1], domain[2]);
+    int lut[256];
+    for (int& v : lut) v = -1;
+    for (int m = 0; m < blob->n_materials; ++m) lut[blob->mat[m].id & 0xFF] = m;
+    if (lut[background_id & 0xFF] < 0) return 2;
+    dom.background = lut[background_id & 0xFF];
+    nvox = 0;
+    for (int k = 0; k < n_grids; ++k) {
+        const midsx_grid_spec& gs = grids[k];
+        if (!gs.ids) return 1;
+        Grid g;
+        g.origin = Vec3(gs.origin[0], gs.origin[1], gs.origin[2]);
+        g.spacing = Vec3(gs.spacing[0], gs.spacing[1], gs.spacing[2]);
+        for (int i = 0; i < 3; ++i) g.dims[i] = gs.dims[i];
+        g.grid_dim = Vec3(g.dims[0] * g.spacing.x, g.dims[1] * g.spacing.y, g.dims[2] * g.spacing.z);
+        g.offset = long(nvox);
+        const size_t nv = size_t(g.dims[0]) * g.dims[1] * g.dims[2];
+        for (size_t i = 0; i < nv; ++i) {
+            if (lut[gs.ids[i]] < 0) return 2;
+            dom.ids.push_back(uint8_t(lut[gs.ids[i]]));
+        }
+        nvox += nv;
+        dom.grids.push_back(g);
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
 /* Runs n histories [first, first + n).  ids are MIDSX material ids (uint8 per voxel).
  * Returns 0 on success, 1 bad argument, 2 unknown material id. */
 int oracle_run(const midsx_table_blob* blob, const midsx_geometry_spec* geom, const uint8_t* ids,
                const midsx_source_spec* src, const midsx_tally_spec* specs, int n_specs, uint64_t seed,
                uint64_t first, uint64_t n, int rng_mode, int n_threads, int max_steps, int max_trials,
                oracle_result* out) {
-    using namespace ref;
     if (!blob || !geom || !ids || !src || !out || n_specs < 0) return 1;
-    InteractionData data = make_interaction_data(blob);
-    ComputationalDomain dom;
-    dom.dim_space = Vec3(geom->domain[0], geom->domain[1], geom->domain[2]);
-    dom.origin = Vec3(geom->origin[0], geom->origin[1], geom->origin[2]);
-    dom.spacing = Vec3(geom->spacing[0], geom->spacing[1], geom->spacing[2]);
-    for (int i = 0; i < 3; ++i) dom.dims[i] = geom->dims[i];
-    dom.grid_dim = Vec3(dom.dims[0] * dom.spacing.x, dom.dims[1] * dom.spacing.y, dom.dims[2] * dom.spacing.z);
-    int lut[256];
-    for (int& v : lut) v = -1;
-    for (int m = 0; m < blob->n_materials; ++m) lut[blob->mat[m].id & 0xFF] = m;
-    if (lut[geom->background_id & 0xFF] < 0) return 2;
-    dom.background = lut[geom->background_id & 0xFF];
-    size_t nvox = size_t(dom.dims[0]) * dom.dims[1] * dom.dims[2];
-    dom.ids.resize(nvox);
-    for (size_t i = 0; i < nvox; ++i) {
-        if (lut[ids[i]] < 0) return 2;
-        dom.ids[i] = uint8_t(lut[ids[i]]);
+    midsx_grid_spec one;
+    std::memset(&one, 0, sizeof(one));
+    for (int i = 0; i < 3; ++i) {
+        one.spacing[i] = geom->spacing[i];
+        one.origin[i] = geom->origin[i];
+        one.dims[i] = geom->dims[i];
     }
+    one.ids = ids;
+    ref::ComputationalDomain dom;
+    size_t nvox = 0;
+    int rc = build_domain(blob, geom->domain, geom->background_id, &one, 1, dom, nvox);
+    if (rc) return rc;
+    return run_domain(blob, dom, nvox, src, specs, n_specs, seed, first, n, rng_mode, n_threads, max_steps,
+                      max_trials, out);
+}
+
+/* Several grids (ComputationalDomain::voxel_grids_, first-hit order); voxels numbered grid
+ * after grid in the dose outputs. */
+int oracle_run_grids(const midsx_table_blob* blob, const double* domain, int background_id,
+                     const midsx_grid_spec* grids, int n_grids, const midsx_source_spec* src,
+                     const midsx_tally_spec* specs, int n_specs, uint64_t seed, uint64_t first, uint64_t n,
+                     int rng_mode, int n_threads, int max_steps, int max_trials, oracle_result* out) {
+    if (!blob || !domain || !grids || n_grids < 1 || !src || !out || n_specs < 0) return 1;
+    ref::ComputationalDomain dom;
+    size_t nvox = 0;
+    int rc = build_domain(blob, domain, background_id, grids, n_grids, dom, nvox);
+    if (rc) return rc;
+    return run_domain(blob, dom, nvox, src, specs, n_specs, seed, first, n, rng_mode, n_threads, max_steps,
+                      max_trials, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size_t nvox, const midsx_source_spec* src,
+               const midsx_tally_spec* specs, int n_specs, uint64_t seed, uint64_t first, uint64_t n, int rng_mode,
+               int n_threads, int max_steps, int max_trials, oracle_result* out) {
+    using namespace ref;
+    InteractionData data = make_interaction_data(blob);
     PhotonSource source;
     source.position = Vec3(src->position[0], src->position[1], src->position[2]);
     source.dir_kind = src->direction_kind;
@@ -929,6 +1006,10 @@ int oracle_run(const midsx_table_blob* blob, const midsx_geometry_spec* geom, co
     }
     return 0;
 }
+
+}  // namespace
+
+extern "C" {
 
 /* Sampler harness for the KS tests: n draws of one sampler with history streams
  * [first, first + n) (Philox) - kind 0 Rayleigh cosine, 1 Compton (cos, E'/E),

@@ -45,7 +45,7 @@ STRUCTS = {
     "midsx_geometry_spec": N.GeometrySpec, "midsx_source_spec": N.SourceSpec,
     "midsx_tally_spec": N.TallySpec, "midsx_run_config": N.RunConfig, "midsx_run_stats": N.RunStats,
     "midsx_batch_job": N.BatchJob, "midsx_server_config": N.ServerConfig, "midsx_request": N.Request,
-    "midsx_request_info": N.RequestInfo, "midsx_server_stats": N.ServerStats,
+    "midsx_request_info": N.RequestInfo, "midsx_server_stats": N.ServerStats, "midsx_grid_spec": N.GridSpec,
 }
 
 

@@ -136,3 +136,52 @@ def test_cpp_hvl_program_reproduces_reference(golden, case, tmp_path):
         sig = ratio * math.sqrt((1 - pa) / (n * pa) + (1 - pb) / (n * pb))
         assert abs(ratio - ref) < 4 * math.hypot(sig, 1e-4), (kind, ratio, ref)
         assert r["primary_energy"] == pytest.approx(e * r["primary_photons"], rel=1e-9)
+
+
+@pytest.mark.gpu
+def test_cpp_multi_grid_program_equals_python_api(tmp_path):
+    """The reference's lead-attenuation scene layout (two lead blocks and a scintillator as
+    three NIfTI grids in one JSON scene) through the C++ API program and through the Python
+    API on the same Philox streams: the mixed form's integer tallies make the AACuboid energy
+    deposition, its photon and interaction counts, and each grid's deposited energy agree to
+    the last bit of the double conversion."""
+    import midsx_gb300 as M
+    from midsx_gb300 import native as N
+    from midsx_gb300 import scenes
+    lead = np.full((82, 25, 5), scenes.LEAD, dtype=np.uint8)      # 0.5 x 2.5 x 8.2 cm at 1 mm
+    scin = np.full((50, 50, 10), scenes.WATER, dtype=np.uint8)    # 1.0 x 5.0 x 5.0 cm at 1 mm
+    grids = [(lead, (0.1, 0.1, 0.1), (0.2, 1.5, 0.0)), (lead, (0.1, 0.1, 0.1), (0.2, 5.2, 0.0)),
+             (scin, (0.1, 0.1, 0.1), (9.65, 0.2, 1.6))]
+    names = ["lead_a.nii", "lead_b.nii", "scin.nii"]
+    for (ids, _, _), name in zip(grids, names):
+        write_nifti(str(tmp_path / name), ids, (1.0, 1.0, 1.0))
+    dim = (10.7, 9.2, 8.2)
+    js = tmp_path / "lead_attenuation.json"
+    entries = ", ".join('{"file_path": "%s", "origin": [%g, %g, %g]}' % (nm, *g[2]) for nm, g in zip(names, grids))
+    js.write_text('{"dim_space": [%g, %g, %g], "background_material_name": "Air, Dry (near sea level)", '
+                  '"voxel_grids": [%s]}' % (*dim, entries))
+    n, seed, energy = 200_000, 7, 100e3
+    scin_o, scin_s = (9.65, 0.2, 1.6), (1.0, 5.0, 5.0)
+    r = subprocess.run([exe("lead_attenuation"), str(js), str(n), str(seed), "1", str(energy), *map(str, scin_o),
+                        *map(str, scin_s)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    out = parse(r.stdout)
+    tables = M.Tables([scenes.AIR, scenes.LEAD, scenes.WATER], e_max=150e3)
+    ph = M.Phantom.from_grids(tables, dim, scenes.AIR, grids)
+    src = M.Source(position=(0, dim[1] / 2, dim[2] / 2), direction=("rect", (10, 0, 0), (0, dim[1], 0), (0, 0, dim[2])),
+                   energy=energy)
+    spec = dict(kind="cuboid", min=scin_o, max=tuple(a + b for a, b in zip(scin_o, scin_s)))
+    tl = M.Tallies(ph, [spec], N.DOSE_FULL)
+    M.run(tables, ph, src, tl, n, seed=seed, first=0, precision="mixed")
+    sc = tl.scalar(0)
+    dep_sum = sum(sc[1 + 3 * c] for c in range(4))
+    dep_cnt = sum(sc[3 * c] for c in range(4))
+    assert float(out["energy_deposition"][0][0]) == pytest.approx(dep_sum, rel=1e-12)
+    assert int(float(out["energy_deposition"][0][1])) == int(dep_cnt)
+    counts = {c[0]: int(float(c[1])) for c in out["count"]}
+    assert counts["NumberOfPhotons"] == int(sum(sc[24 + c] for c in range(4)))
+    assert counts["NumberOfInteractions"] == int(sum(sc[28 + c] for c in range(4)))
+    dose = tl.dose()["sum"]
+    for k in range(3):
+        assert float(out["grid_deposit"][k][1]) == pytest.approx(dose[k].sum(), rel=1e-12), k
+    assert dose[0].sum() > 0 and dose[2].sum() > 0

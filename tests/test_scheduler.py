@@ -107,3 +107,32 @@ def test_bad_scheduler_and_block_rejected(scene):
     with pytest.raises(N.MidsxError) as e:
         M.run(tables, ph, src, tl, 10, seed=1, scheduler="pool", block=256)
     assert e.value.status == N.INVALID_ARG
+
+
+def test_pool_aggregates_shared_records():
+    """A 2x2x2-voxel water phantom under a pencil beam: most collisions of a warp deposit into
+    the same few dose records and cross the same detector bins and scalar tallies, so the
+    warp-aggregated atomics sum large peer groups; the integer totals must still equal those
+    of one atomic per lane."""
+    ids = np.full((2, 2, 2), scenes.WATER, dtype=np.uint8)
+    tables = M.Tables([scenes.AIR, scenes.WATER], e_max=100e3)
+    ph = M.Phantom(tables, (20, 20, 20), (5, 5, 5), (5, 5, 5), ids, scenes.AIR)
+    src = M.Source(position=(10, 10, 0), direction=("beam", (10, 10, 20)), energy=60e3)
+    specs = [dict(kind="binned", corner=(5, 5, 19), edge1=(10, 0, 0), edge2=(0, 10, 0), nu=2, nv=2),
+             dict(kind="disc", center=(10, 10, 18), normal=(0, 0, 1), radius=8.0),
+             dict(kind="cuboid", min=(5, 5, 5), max=(15, 15, 15))]
+    out = {}
+    for sched in ("lanes", "pool"):
+        tl = M.Tallies(ph, specs, N.DOSE_FULL)
+        M.run(tables, ph, src, tl, 50_000, seed=21, precision="mixed", scheduler=sched)
+        out[sched] = (tl.dose(), tl.binned(0), tl.scalar(1), tl.scalar(2), tl.stats())
+    a, b = out["lanes"], out["pool"]
+    for k in ("sum", "sumsq", "count"):
+        np.testing.assert_array_equal(a[0][k], b[0][k])
+    for x, y in zip(a[1], b[1]):
+        np.testing.assert_array_equal(x, y)
+    np.testing.assert_array_equal(a[2], b[2])
+    np.testing.assert_array_equal(a[3], b[3])
+    for k in EXACT_STATS:
+        assert a[4][k] == b[4][k], k
+    assert a[0]["count"].sum() > 1000 and a[2][0] > 0
