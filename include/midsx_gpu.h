@@ -264,6 +264,18 @@ typedef enum midsx_scheduler {
     MIDSX_SCHED_POOL = 2
 } midsx_scheduler;
 
+/* Flight sampling.  REFERENCE: Woodcock tracking against the global majorant everywhere
+ * (src/MIDSX/Core/physics_engine.cpp:28-79, interaction_data.cpp:42-73).  BACKGROUND_FAST:
+ * outside every voxel grid the medium is the background material alone, so its own
+ * attenuation is an exact majorant there: a flight that starts in the background is sampled
+ * with it and ends at a real collision, at the first grid it enters, or out of the domain.
+ * Unbiased (same distributions) but not the reference's random-number use, so results agree
+ * with REFERENCE statistically, not history by history.  Photon-pool scheduler only. */
+typedef enum midsx_tracking {
+    MIDSX_TRACK_REFERENCE = 0,
+    MIDSX_TRACK_BACKGROUND_FAST = 1
+} midsx_tracking;
+
 typedef struct midsx_run_config {
     int32_t precision;           /* midsx_precision */
     int32_t max_steps;           /* per-history step cap (0 = 100000) */
@@ -275,6 +287,8 @@ typedef struct midsx_run_config {
     int32_t chunk;               /* lane-parking scheduler: history ids a lane reserves per fetch
                                     (0 = 1) */
     int32_t scheduler;           /* midsx_scheduler */
+    int32_t tracking;            /* midsx_tracking */
+    int32_t reserved;
     uint64_t seed;
     uint64_t first_history;      /* history ids [first, first + n) select Philox streams */
     uint64_t n_histories;

@@ -337,9 +337,13 @@ PRECISIONS = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}
 SCHEDULERS = {"default": N.SCHED_DEFAULT, "lanes": N.SCHED_LANES, "pool": N.SCHED_POOL}
 
 
+TRACKING = {"reference": N.TRACK_REFERENCE, "background_fast": N.TRACK_BACKGROUND_FAST}
+
+
 def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0, regroup=0,
-               chunk=0, scheduler="default"):
+               chunk=0, scheduler="default", tracking="reference"):
     c = N.RunConfig()
+    c.tracking = TRACKING[tracking] if isinstance(tracking, str) else int(tracking)
     c.regroup = int(regroup)
     c.chunk = int(chunk)
     c.scheduler = SCHEDULERS[scheduler] if isinstance(scheduler, str) else int(scheduler)

@@ -140,6 +140,50 @@ __device__ Geo<R> make_geo(const DevGeom& G) {
     return g;
 }
 
+// Distance along the ray p + t d (t >= 0) to the closed box [lo, lo + ext], +inf if the ray
+// misses it (slab method); 0 if p is inside.
+template <typename R>
+__device__ __forceinline__ R box_entry(const V3<R>& p, const V3<R>& d, const V3<R>& lo, const V3<R>& ext) {
+    R tmin = R(0), tmax = R(INFINITY);
+    const R pp[3] = {p.x, p.y, p.z}, dd[3] = {d.x, d.y, d.z}, ll[3] = {lo.x, lo.y, lo.z}, ee[3] = {ext.x, ext.y, ext.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (dd[a] == R(0)) {
+            if (pp[a] < ll[a] || pp[a] > ll[a] + ee[a]) return R(INFINITY);
+            continue;
+        }
+        R t1 = (ll[a] - pp[a]) / dd[a], t2 = (ll[a] + ee[a] - pp[a]) / dd[a];
+        if (t1 > t2) {
+            const R t = t1;
+            t1 = t2;
+            t2 = t;
+        }
+        tmin = t1 > tmin ? t1 : tmin;
+        tmax = t2 < tmax ? t2 : tmax;
+    }
+    return tmin <= tmax ? tmin : R(INFINITY);
+}
+
+// Distance along a ray from the background to the first grid box it enters, +inf if none.
+template <typename R, bool MX>
+__device__ __forceinline__ R grid_entry(const Geo<R>& g, const V3<R>& p, const V3<R>& d) {
+    R best = box_entry<R>(p, d, g.org, g.ext);
+    for (int k = 0; k + 1 < g.n_grids; ++k) {
+        const DevGrid& G = g.extra[k];
+        V3<R> o, e;
+        if constexpr (MX) {
+            o = {G.f_origin[0], G.f_origin[1], G.f_origin[2]};
+            e = {G.f_ext[0], G.f_ext[1], G.f_ext[2]};
+        } else {
+            o = {G.origin[0], G.origin[1], G.origin[2]};
+            e = {G.ext[0], G.ext[1], G.ext[2]};
+        }
+        const R t = box_entry<R>(p, d, o, e);
+        best = t < best ? t : best;
+    }
+    return best;
+}
+
 // ComputationalDomain::getVoxel (computational_domain.cpp:23-31) for a point of the domain:
 // the first grid whose closed box holds the point gives the voxel - vox is its number in the
 // phantom (grid after grid), mat its material - else the background (vox = -1).  Inside a grid

@@ -66,8 +66,13 @@ __host__ __device__ inline size_t pool_smem(int n_jobs, bool multi, int n_materi
            size_t(block / 32) * 2 * kPoolSlots;
 }
 
-template <typename R, bool MULTI>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_kernel(const RunParams P) {
+// FAST = MIDSX_TRACK_BACKGROUND_FAST (a kernel of its own: compiled into one kernel with the
+// reference tracking, the fast path's code cost the reference path 8 %).  Batched launches
+// take blocks of up to 256 threads: their per-job counters and geometry in shared memory
+// (~16 KB for 64 jobs) are then shared by twice the photon slots.
+template <typename R, bool MULTI, bool FAST>
+__global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3 : 6) : (MULTI ? 2 : 4))
+    transport_pool_kernel(const RunParams P) {
     constexpr bool MX = sizeof(R) == 4;
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -121,6 +126,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
     const Geo<R> g0 = make_geo<R>(P.job0.G);
     const unsigned long long epoch = P.epoch ? *P.epoch : 0ull;
     const int regroup = max(1, min(P.regroup, 32));
+    constexpr bool fast_mode = FAST;
     int rdy_top = 0, ev_top = kPoolSlots;  // warp-uniform list sizes
     bool exhausted = false;                // warp-uniform: every history of the launch handed out
 
@@ -158,6 +164,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
         steps = S.steps[sl];
         fetches = S.fetches[sl];
         words = S.words[sl];
+        // fast tracking steers by the last lookup's region (-1: background, -2: not known)
+        if constexpr (fast_mode) vox = int(S.vox[sl]);
         ntal = MULTI ? P.jobs[job].n_tallies : P.job0.n_tallies;
     };
     auto load_event = [&](int sl) {  // a parked photon: flight state plus its collision site
@@ -175,6 +183,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
         S.steps[sl] = steps;
         S.fetches[sl] = fetches;
         S.words[sl] = words;
+        if constexpr (fast_mode) S.vox[sl] = uint32_t(vox);
     };
     auto save_collision = [&](int sl) {  // a photon parked at a real collision
         save_flight(sl);
@@ -230,10 +239,24 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                 ++steps;
                 uint64_t w1, w2;
                 rng.next_pair64(w1, w2);
-                if constexpr (MX)
+                // MIDSX_TRACK_BACKGROUND_FAST: a photon known to be in the background (vox == -1
+                // after its last voxel lookup) flies against the background's own attenuation,
+                // exact there, up to the first grid it would enter
+                const bool fast = fast_mode && vox == -1;
+                R lim = R(INFINITY);  // distance to the first grid on the way (fast flights)
+                if (fast) {
+                    const R mu_bg = S.mu[g.bg * ns + cur];
+                    if constexpr (MX)
+                        s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) / mu_bg;
+                    else
+                        s = -log_(to_uniform(w1, R(0))) / mu_bg;
+                    lim = grid_entry<R, MX>(g, pos, dir);
+                    if (lim <= s) s = lim;
+                } else if constexpr (MX) {
                     s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) * inv_mu_max;
-                else
+                } else {
                     s = -log_(to_uniform(w1, R(0))) / mu_max;
+                }
                 p0 = pos;
                 pos = {pos.x + s * dir.x, pos.y + s * dir.y, pos.z + s * dir.z};
                 if (!(pos.x >= R(0) && pos.x <= g.dom.x && pos.y >= R(0) && pos.y <= g.dom.y && pos.z >= R(0) &&
@@ -241,6 +264,17 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                     stat_add(st, kStEscE, fx_stat(E));
                     segment = true;
                     park = kKindStart;
+                } else if (fast) {
+                    mat = g.bg;
+                    if (s == lim) {
+                        // on a grid face, no interaction: the next flight is a reference step
+                        // (global majorant, valid everywhere) from here
+                        vox = -2;
+                        segment = true;
+                    } else {
+                        vox = -1;
+                        park = kKindCollide;  // every background collision is real
+                    }
                 } else {
                     locate<R, MX>(g, pos, vox, mat, fetches, st);
                     if (to_uniform(w2, R(0)) < S.thr[mat * ns + cur])
@@ -423,7 +457,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) transport_pool_ke
                     n_coh = n_incoh = 0;
                     steps = fetches = trials = words = 0;
                     mat = 0;
-                    vox = -1;
+                    vox = -2;  // region of the source point not looked up yet
                     s = R(0);
                     p0 = pos;
                     need_refresh = true;

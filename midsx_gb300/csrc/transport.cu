@@ -108,6 +108,7 @@ struct RunParams {
     unsigned long long total;               // histories of this launch
     const unsigned long long* epoch;        // optional: history ids advance by n per epoch
     int max_steps, max_trials;
+    int tracking;   // midsx_tracking
     int regroup;    // lanes of a warp that wait for an event before the warp runs the events
     int chunk;      // histories a lane reserves per fetch
     double* trace;  // optional (single job): energy deposited in grid voxels per history
@@ -1156,16 +1157,17 @@ midsx_status launch_typed(midsx_tables_h tables, const RunParams& P, const midsx
     return MIDSX_OK;
 }
 
-template <typename R, bool MULTI>
+template <typename R, bool MULTI, bool FAST>
 midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_run_config& cfg, int block,
                          cudaStream_t s) {
     const size_t smem = pool_smem<R>(P.n_jobs, MULTI, tables->T.n_materials, block);
     if (smem > 48 * 1024)
-        CUDA_TRY(cudaFuncSetAttribute(transport_pool_kernel<R, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(smem)));
+        CUDA_TRY(cudaFuncSetAttribute(transport_pool_kernel<R, MULTI, FAST>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = cfg.blocks_per_sm;
     if (per_sm <= 0) {
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_pool_kernel<R, MULTI>, block, smem));
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_pool_kernel<R, MULTI, FAST>, block,
+                                                               smem));
         per_sm = std::max(per_sm, 1);
     }
     if (per_sm < 1) {
@@ -1175,9 +1177,16 @@ midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_
     // a warp keeps two photons per lane in flight
     uint64_t want = (P.total + 2 * uint64_t(block) - 1) / (2 * uint64_t(block));
     uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(tables->sm_count) * per_sm));
-    transport_pool_kernel<R, MULTI><<<unsigned(grid), block, smem, s>>>(P);
+    transport_pool_kernel<R, MULTI, FAST><<<unsigned(grid), block, smem, s>>>(P);
     CUDA_TRY(cudaGetLastError());
     return MIDSX_OK;
+}
+
+template <typename R, bool MULTI>
+midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_run_config& cfg, int block,
+                         cudaStream_t s) {
+    return P.tracking == MIDSX_TRACK_BACKGROUND_FAST ? launch_pool<R, MULTI, true>(tables, P, cfg, block, s)
+                                                     : launch_pool<R, MULTI, false>(tables, P, cfg, block, s);
 }
 
 // Completes the launch parameters from cfg, zeroes the history counter and launches.  The
@@ -1188,18 +1197,27 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
         set_last_error("unknown scheduler");
         return MIDSX_INVALID_ARG;
     }
+    if (cfg.tracking != MIDSX_TRACK_REFERENCE && cfg.tracking != MIDSX_TRACK_BACKGROUND_FAST) {
+        set_last_error("unknown tracking");
+        return MIDSX_INVALID_ARG;
+    }
     const bool pool = cfg.scheduler != MIDSX_SCHED_LANES && P.trace == nullptr &&
                       (cfg.scheduler == MIDSX_SCHED_POOL || kDefaultScheduler == MIDSX_SCHED_POOL);
+    if (cfg.tracking == MIDSX_TRACK_BACKGROUND_FAST && !pool) {
+        set_last_error("background fast tracking runs in the photon-pool scheduler only");
+        return MIDSX_INVALID_ARG;
+    }
+    P.tracking = cfg.tracking;
     P.max_steps = cfg.max_steps > 0 ? cfg.max_steps : 100000;
     P.max_trials = cfg.max_compton_trials > 0 ? cfg.max_compton_trials : 100000;
     P.regroup = cfg.regroup > 0 ? std::min(cfg.regroup, 32) : (pool ? 32 : 24);
     P.chunk = cfg.chunk > 0 ? std::min(cfg.chunk, 64) : 1;
     const bool mixed = cfg.precision == MIDSX_PREC_MIXED;
-    const int max_block = pool ? 128 : 256;
+    const int max_block = pool && !multi ? 128 : 256;
     int block = cfg.block_size > 0 ? cfg.block_size : max_block;
     if (block > max_block || block % 32) {
-        set_last_error(pool ? "block_size must be a multiple of 32 up to 128 (photon pool)"
-                            : "block_size must be a multiple of 32 up to 256");
+        set_last_error(max_block == 128 ? "block_size must be a multiple of 32 up to 128 (photon pool, one job)"
+                                        : "block_size must be a multiple of 32 up to 256");
         return MIDSX_INVALID_ARG;
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1755,7 +1773,7 @@ extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precis
                     }
         c.scheduler = MIDSX_SCHED_POOL;
         c.chunk = 0;
-        for (int bs : {64, 96, 128})
+        for (int bs : {64, 128, 256})
             for (int ps : {0})
                 for (int rg : {24, 28, 32}) {
                     c.block_size = bs;

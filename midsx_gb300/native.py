@@ -16,6 +16,7 @@ SCALAR_SLOTS = 40
 OK, INVALID_ARG, OOM, TIMEOUT, STEP_CAP, TABLE_RANGE, CUDA_ERROR, NOT_FOUND, IO_ERROR = range(9)
 PREC_FP64, PREC_MIXED = 0, 1
 SCHED_DEFAULT, SCHED_LANES, SCHED_POOL = 0, 1, 2
+TRACK_REFERENCE, TRACK_BACKGROUND_FAST = 0, 1
 DIR_BEAM, DIR_ISOTROPIC, DIR_RECTANGLE, DIR_DISC = range(4)
 SPEC_MONO, SPEC_POLY = 0, 1
 TALLY_DISC, TALLY_RECT, TALLY_BINNED_RECT, TALLY_AACUBOID = 1, 2, 3, 4
@@ -82,7 +83,8 @@ class RunConfig(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_steps", C.c_int32),
                 ("max_compton_trials", C.c_int32), ("block_size", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("regroup", C.c_int32), ("chunk", C.c_int32),
-                ("scheduler", C.c_int32), ("seed", C.c_uint64),
+                ("scheduler", C.c_int32), ("tracking", C.c_int32), ("reserved", C.c_int32),
+                ("seed", C.c_uint64),
                 ("first_history", C.c_uint64), ("n_histories", C.c_uint64)]
 
 

@@ -99,7 +99,7 @@ def test_autotune_picks_a_shape_and_resets_tallies(setup):
     launch, rate = batch.autotune("mixed", trial=200_000)
     assert rate > 0
     if launch["scheduler"] == N.SCHED_POOL:
-        assert launch["block"] in (64, 96, 128) and 24 <= launch["regroup"] <= 32
+        assert launch["block"] in (64, 128, 256) and 24 <= launch["regroup"] <= 32
     else:
         assert launch["scheduler"] == N.SCHED_LANES
         assert launch["block"] in (128, 256) and 12 <= launch["regroup"] <= 28 and launch["chunk"] in (1, 4)
