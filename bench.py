@@ -42,6 +42,8 @@ def parse():
     p.add_argument("--batch-scale", type=float, default=1.0, help="history scale of the batched jobs")
     p.add_argument("--serving", type=int, default=1, help="run the serving leg (1/0)")
     p.add_argument("--serving-requests", type=int, default=120, help="requests at 200/s in the serving leg")
+    p.add_argument("--radiography", type=int, default=1, help="run the radiography precision-ablation leg (1/0)")
+    p.add_argument("--radiography-histories", type=float, default=1e6, help="histories per precision (radiography)")
     return p.parse_args()
 
 
@@ -305,6 +307,8 @@ def main():
         result["e2e"] = None
     if not args.quick:
         result["background_fast_tracking"] = fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, N_hist)
+    if not args.quick and args.radiography:
+        result["radiography_precision_ablation"] = radiography_leg(args, np, torch)
     if not args.quick and args.batched:
         result["batched"] = batched_leg(args, torch)
     if not args.quick and args.serving:
@@ -347,6 +351,59 @@ def fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, n_hist):
             "dose_vs_reference_tracking": {"histories": ncmp, "voxels_compared": int(sel.sum()),
                                            "frac_voxels_beyond_3sigma": float(np.mean(np.abs(z) > 3)),
                                            "total_rel_diff": float(abs(s1.sum() - s2.sum()) / s1.sum())}}
+
+
+def radiography_leg(args, np, torch):
+    """Config 3, the precision ablation: the 512x512x256 radiography phantom at 0.5 mm (40
+    ellipsoids and sixteen 2 mm lead spheres), 100 kVp, 512^2 detector of 1 mm bins at 100 cm
+    SID, primary and scattered fluence per bin - the mixed and the FP64 path on identical
+    Philox streams, on a bounded history count (the reference algorithm needs ~17.5k Woodcock
+    steps per history here: lead sets the global majorant along the whole 100 cm), plus the
+    opt-in background fast tracking."""
+    import midsx_gb300 as M
+    from midsx_gb300 import scenes
+    t0 = time.time()
+    sc = scenes.radiography(n_histories=1)
+    tables, ph, src, tl = sc.build()
+    log("radiography setup %.1fs" % (time.time() - t0))
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(n, precision, tracking="reference", seed=5):
+        tl.reset(sptr)
+        ev[0].record(stream)
+        M.run(tables, ph, src, tl, n, seed=seed, precision=precision, stream=sptr, tracking=tracking)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]) / 1e3
+
+    n = int(args.radiography_histories)
+    timed(n // 10, "mixed")  # warm-up
+    images, out = {}, {}
+    for precision in ("mixed", "fp64"):
+        dt = timed(n, precision)
+        e, c = tl.binned(0, sptr)
+        images[precision] = e
+        st = tl.stats(sptr)
+        out[precision] = {"value": n / dt, "unit": UNIT, "steps_per_history": st["steps"] / st["histories"]}
+    # identical streams: primary (class 0) and scattered (classes 1-3) energy per bin
+    a, b = images["mixed"], images["fp64"]
+    prim_a, prim_b = a[..., 0].ravel(), b[..., 0].ravel()
+    scat_a, scat_b = a[..., 1:].sum(axis=2).ravel(), b[..., 1:].sum(axis=2).ravel()
+    hit = prim_b > 0
+    rel = np.abs(prim_a[hit] - prim_b[hit]) / prim_b[hit]
+    fast_dt = timed(n, "mixed", tracking="background_fast", seed=6)
+    fst = tl.stats(sptr)
+    return {"workload": sc.name + " (512^2 detector at 100 cm SID, 16 Pb spheres)", "histories": n,
+            "mixed": out["mixed"], "fp64": out["fp64"], "mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"],
+            "identical_streams": {
+                "primary_total_rel_diff": float(abs(prim_a.sum() - prim_b.sum()) / prim_b.sum()),
+                "scatter_total_rel_diff": float(abs(scat_a.sum() - scat_b.sum()) / scat_b.sum()),
+                "primary_bins_identical": float(np.mean(prim_a[hit] == prim_b[hit])) if hit.any() else None,
+                "primary_bins_rel_diff_p99": float(np.percentile(rel, 99)) if hit.any() else None},
+            "background_fast_tracking": {"value": n / fast_dt, "unit": UNIT,
+                                         "steps_per_history": fst["steps"] / fst["histories"]}}
 
 
 def batched_leg(args, torch):

@@ -49,6 +49,13 @@ public:
     double interpolateIncoherentScatteringCrossSection(double energy) const { return eval(3, energy); }
     double interpolateIncoherentScatteringFunction(double x) const { return eval(4, x); }
     double interpolateCoherentFormFactor(double x) const { return eval(5, x); }
+    // mu_en/rho, cm2/g (reference: material_data.h:143).  The reference's table comes from
+    // NIST via its database; without one it follows from the built tables and the
+    // transport's deposition model (midsx_tables_mu_en).  A table set here - (energy eV,
+    // mu_en/rho cm2/g) pairs, ascending - is interpolated LogLogLinear, clamped at its ends,
+    // as the reference interpolates its own.
+    double interpolateMassEnergyAbsorptionCoefficient(double energy) const;
+    void setMassEnergyAbsorptionCoefficients(std::vector<std::pair<double, double>> table);
     // Rayleigh cosine by RITA inversion with a host uniform (src/MIDSX/Core/probability_dist.cpp:73-88).
     double sampleCoherentScatteringDCS(double energy) const;
     // (x, y) node table of one interpolator: 0 total, 1 photo, 4 S(x), 5 F(x)
@@ -60,6 +67,7 @@ private:
     double eval(int which, double x) const;
     std::shared_ptr<midsx::BlobHolder> blob_;
     int index_ = 0;
+    std::vector<std::pair<double, double>> mu_en_table_;
 };
 
 class Material {

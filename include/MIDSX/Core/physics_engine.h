@@ -57,7 +57,7 @@ private:
     midsx_run_stats stats_{};
     std::vector<double> dose_sum_, dose_sumsq_, dose_count_;
     bool dose_pending_ = false;
-    void ensureDevice();
+    void ensureDevice(const midsx_source_spec& first_source);
 };
 
 void runSimulation(PhotonSource& source, PhysicsEngine& physics_engine,

@@ -17,10 +17,19 @@ public:
     virtual ~SurfaceTally() = default;
     SurfaceQuantityContainer& getSurfaceQuantityContainer() { return surface_quantities_; }
     virtual midsx_tally_spec describe() const;
+    // Incident-energy spectrum bins of a disc or rectangle (IncidentSpectrum).  Without a
+    // call, a tally whose container holds IncidentEnergy gets bins centred on the energies of
+    // the source of the engine's first run (one bin per spectrum line), which puts every
+    // primary photon at a bin centre.
+    void setEnergyBins(double e_min, double e_width, int n);
+    bool hasEnergyBins() const { return n_energy_ > 0; }
 
 protected:
     Vec3 norm_;
     SurfaceQuantityContainer surface_quantities_;
+    double e_min_ = 0, e_width_ = 0;
+    int n_energy_ = 0;
+    void describeSpectrum(midsx_tally_spec& s) const;
 };
 
 class DiscSurfaceTally : public SurfaceTally {

@@ -135,6 +135,18 @@ midsx_status midsx_tables_rita(const midsx_table_blob* blob, int32_t material, d
 midsx_status midsx_tables_eval(const midsx_table_blob* blob, int32_t material, int32_t which,
                                const double* x, double* y, int64_t n);
 
+/* Mass energy-absorption coefficient mu_en/rho (cm2/g) of `material` at energies x (eV),
+ * the coefficient MaterialData::interpolateMassEnergyAbsorptionCoefficient returns
+ * (include/MIDSX/Core/material_data.h:143) for DerivedQuantity::getPrimaryAirKerma.  The
+ * reference reads NIST tables from its database; here it follows from the built tables and
+ * the transport's own deposition model: a photoelectric absorption deposits the photon's
+ * energy, an incoherent scatter the electron's share of it (src/MIDSX/Core/
+ * photon_interactions.cpp:43-141), so mu_en = mu_photo + mu_incoh * <1 - k'/k>, the mean over
+ * the Klein-Nishina x S(x) angular distribution (Gauss-Legendre quadrature over cos theta).
+ * Fluorescence escape and bremsstrahlung are not modelled by the transport and not here. */
+midsx_status midsx_tables_mu_en(const midsx_table_blob* blob, int32_t material, const double* x, double* y,
+                                int64_t n);
+
 const char* midsx_status_string(midsx_status s);
 const char* midsx_last_error(void);
 
@@ -223,6 +235,11 @@ midsx_status midsx_gpu_source_destroy(midsx_source_h s);
  *   EnergyDeposition[3x4], IncidentEnergy[3x4], NumberOfPhotons[4], NumberOfInteractions[4]
  * BINNED_RECT is a RECT split into nu x nv bins (bin (i,j) equals a RectangularSurfaceTally
  * over that cell); per bin and class it holds the incident energy sum and photon count.
+ * A DISC or RECT with n_energy > 0 also keeps an incident-energy spectrum: n_energy bins
+ * [e_min + k e_width, e_min + (k+1) e_width) eV, per bin and class the number of crossings
+ * and the sum of their entrance cosines.  It replaces the raw IncidentEnergy/EntranceCosine
+ * vectors that DerivedQuantity::getPrimaryFluence scans (src/MIDSX/Core/derived_quantities.cpp:
+ * 3-45): with bins centred on the source's energies every primary photon sits at a bin centre.
  * The voxel dose tally (per grid voxel: deposit count, sum, sum of squares - the summary
  * of the reference's Voxel::dose VectorValue) is enabled by dose_mode. */
 typedef enum midsx_tally_kind {
@@ -238,12 +255,15 @@ typedef enum midsx_dose_mode {
     MIDSX_DOSE_FULL = 2      /* count, sum and sum of squares per voxel */
 } midsx_dose_mode;
 
+#define MIDSX_MAX_ENERGY_BINS 65536
+
 typedef struct midsx_tally_spec {
     int32_t kind;
     int32_t nu, nv;          /* bins of a BINNED_RECT along edge1, edge2 */
-    int32_t reserved;
+    int32_t n_energy;        /* DISC / RECT: incident-energy spectrum bins (0 = none) */
     double a[3], b[3], c[3];
     double radius;
+    double e_min, e_width;   /* spectrum: lower edge and bin width (eV) */
 } midsx_tally_spec;
 
 #define MIDSX_SCALAR_SLOTS 40  /* doubles returned per scalar tally, see midsx_gpu_fetch_scalar */
@@ -328,6 +348,10 @@ midsx_status midsx_gpu_fetch_scalar(midsx_tallies_h t, int32_t index, double* ou
  * count[nu*nv*4]. */
 midsx_status midsx_gpu_fetch_binned(midsx_tallies_h t, int32_t index, double* energy,
                                     double* count, void* stream);
+/* Incident-energy spectrum of surface tally `index` (n_energy > 0): count[n_energy*4] and
+ * cosine[n_energy*4] ([energy bin][class]; either may be NULL). */
+midsx_status midsx_gpu_fetch_spectrum(midsx_tallies_h t, int32_t index, double* count, double* cosine,
+                                      void* stream);
 
 /* One call from host memory to host memory: uploads the phantom ids, runs, and reads the
  * dose sum and statistics back (the end-to-end form used by the C++ runSimulation). */

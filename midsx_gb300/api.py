@@ -66,6 +66,16 @@ class TableBlob:
                 "midsx_tables_eval")
         return y
 
+    def mu_en(self, material, energies):
+        """Mass energy-absorption coefficient mu_en/rho (cm2/g) of dense material `material` at
+        `energies` (eV): photoelectric plus the electron's mean share of incoherent scatters
+        under the transport's own sampling density (midsx_tables_mu_en)."""
+        e = np.ascontiguousarray(energies, dtype=np.float64)
+        y = np.empty_like(e)
+        N.check(N.load().midsx_tables_mu_en(self.ptr, int(material), N.dptr(e), N.dptr(y), e.size),
+                "midsx_tables_mu_en")
+        return y
+
     def dense_index(self, mid):
         return self.ids.index(mid)
 
@@ -235,11 +245,14 @@ class Source:
 
 
 def tally_specs(specs):
-    """specs: list of dicts {kind: 'disc'|'rect'|'binned'|'cuboid', ...}."""
+    """specs: list of dicts {kind: 'disc'|'rect'|'binned'|'cuboid', ...}; a disc or rect may
+    add spectrum=(e_min, e_width, n_energy) for an incident-energy spectrum."""
     arr = (N.TallySpec * max(1, len(specs)))()
     for i, d in enumerate(specs):
         t = arr[i]
         k = d["kind"]
+        if d.get("spectrum") is not None:
+            t.e_min, t.e_width, t.n_energy = float(d["spectrum"][0]), float(d["spectrum"][1]), int(d["spectrum"][2])
         if k == "disc":
             t.kind = N.TALLY_DISC
             t.a, t.b, t.radius = N.vec3(d["center"]), N.vec3(d["normal"]), float(d["radius"])
@@ -318,6 +331,17 @@ class Tallies:
         N.check(N.load().midsx_gpu_fetch_binned(self.handle, int(i), N.dptr(e), N.dptr(c), stream),
                 "midsx_gpu_fetch_binned")
         return e.reshape(d["nv"], d["nu"], 4), c.reshape(d["nv"], d["nu"], 4)
+
+    def spectrum(self, i, stream=None):
+        """Incident-energy spectrum of surface tally i: (count, cosine_sum), each shaped
+        (n_energy, 4) - energy bin by scatter class (0 primary, 1 single coherent, 2 single
+        incoherent, 3 multiple)."""
+        n = int(self.specs[i]["spectrum"][2])
+        c = np.empty(n * 4)
+        s = np.empty(n * 4)
+        N.check(N.load().midsx_gpu_fetch_spectrum(self.handle, int(i), N.dptr(c), N.dptr(s), stream),
+                "midsx_gpu_fetch_spectrum")
+        return c.reshape(n, 4), s.reshape(n, 4)
 
     def close(self):
         if self.handle:

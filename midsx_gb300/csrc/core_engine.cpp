@@ -3,7 +3,9 @@
 // The history loop itself runs in the transport kernel behind the C ABI; this file moves
 // the API objects to the device once, launches, and writes the device sums back into the
 // reference's result objects.
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -18,6 +20,33 @@ void check(midsx_status s, const char* what) {
     if (s == MIDSX_INVALID_ARG) throw std::invalid_argument(msg);
     throw std::runtime_error(msg);
 }
+
+// Spectrum bins centred on a source's energies: one bin per line of a spectrum on an even
+// grid (the reference's CSV spectra), a 1 eV bin around a single energy.  Lines off the grid
+// of the smallest spacing still land in the bin that holds them.
+void default_energy_bins(const midsx_source_spec& src, midsx_tally_spec& s) {
+    if (src.spectrum_kind != MIDSX_SPEC_POLY || src.n_bins < 2 || !src.bin_energy) {
+        const double e = src.spectrum_kind == MIDSX_SPEC_POLY && src.n_bins == 1 && src.bin_energy
+                             ? src.bin_energy[0] : src.mono_energy;
+        s.n_energy = 1;
+        s.e_width = 1.0;
+        s.e_min = e - 0.5;
+        return;
+    }
+    std::vector<double> e(src.bin_energy, src.bin_energy + src.n_bins);
+    std::sort(e.begin(), e.end());
+    double step = 0;
+    for (size_t i = 1; i < e.size(); ++i) {
+        const double d = e[i] - e[i - 1];
+        if (d > 0 && (step == 0 || d < step)) step = d;
+    }
+    if (step == 0) step = 1.0;
+    const double span = (e.back() - e.front()) / step;
+    s.e_width = step;
+    s.e_min = e.front() - 0.5 * step;
+    s.n_energy = int(std::min<double>(MIDSX_MAX_ENERGY_BINS, std::floor(span + 0.5) + 1));
+}
+
 }  // namespace
 
 struct PhysicsEngine::Device {
@@ -25,6 +54,7 @@ struct PhysicsEngine::Device {
     midsx_phantom_h phantom = nullptr;
     midsx_tallies_h tallies = nullptr;
     std::vector<int> spec_kind;
+    std::vector<midsx_tally_spec> specs;
     ~Device() {
         if (tallies) midsx_gpu_tallies_destroy(tallies);
         if (phantom) midsx_gpu_phantom_destroy(phantom);
@@ -47,7 +77,7 @@ void PhysicsEngine::addSurfaceTallies(std::vector<std::unique_ptr<SurfaceTally>>
     for (auto& t : s) surface_tallies_.push_back(std::move(t));
 }
 
-void PhysicsEngine::ensureDevice() {
+void PhysicsEngine::ensureDevice(const midsx_source_spec& first_source) {
     if (dev_) return;
     if (!interaction_data_.blob()) throw std::invalid_argument("InteractionData has no materials");
     const int n_grids = comp_domain_.getNumVoxelGrids();
@@ -78,17 +108,25 @@ void PhysicsEngine::ensureDevice() {
                                          n_grids, &d->phantom),
           "midsx_gpu_phantom_create_grids");
     std::vector<midsx_tally_spec> specs;
-    for (auto& t : surface_tallies_) specs.push_back(t->describe());
+    for (auto& t : surface_tallies_) {
+        midsx_tally_spec s = t->describe();
+        // a disc or rectangle measuring IncidentEnergy keeps a spectrum for DerivedQuantity
+        if (s.kind != MIDSX_TALLY_SURFACE_BINNED_RECT && !t->hasEnergyBins() &&
+            t->getSurfaceQuantityContainer().getVectorQuantities().count(VectorSurfaceQuantityType::IncidentEnergy))
+            default_energy_bins(first_source, s);
+        specs.push_back(s);
+    }
     for (auto& t : volume_tallies_) specs.push_back(t->describe());
     for (auto& s : specs) d->spec_kind.push_back(s.kind);
+    d->specs = specs;
     check(midsx_gpu_tallies_create(d->phantom, specs.data(), int32_t(specs.size()), MIDSX_DOSE_FULL, &d->tallies),
           "midsx_gpu_tallies_create");
     dev_ = std::move(d);
 }
 
 double PhysicsEngine::run(PhotonSource& source, uint64_t n_photons) {
-    ensureDevice();
     midsx_source_spec spec = source.describe();
+    ensureDevice(spec);
     midsx_source_h src = nullptr;
     check(midsx_gpu_source_create(&spec, &src), "midsx_gpu_source_create");
     midsx_run_config cfg;
@@ -128,6 +166,17 @@ double PhysicsEngine::run(PhotonSource& source, uint64_t n_photons) {
             }
             for (auto& q : c.getCountQuantities())
                 for (int cls = 0; cls < 4; ++cls) q.second.getClassValues(cls).count_ = (long long)slots[24 + cls];
+            const midsx_tally_spec& ts = dev_->specs[k];
+            if (ts.n_energy > 0) {
+                IncidentSpectrum& sp = c.getIncidentSpectrum();
+                sp.e_min = ts.e_min;
+                sp.e_width = ts.e_width;
+                sp.n = ts.n_energy;
+                sp.count.assign(size_t(ts.n_energy) * 4, 0.0);
+                sp.cosine.assign(size_t(ts.n_energy) * 4, 0.0);
+                check(midsx_gpu_fetch_spectrum(dev_->tallies, int32_t(k), sp.count.data(), sp.cosine.data(), nullptr),
+                      "midsx_gpu_fetch_spectrum");
+            }
         }
         ++k;
     }

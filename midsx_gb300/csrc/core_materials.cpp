@@ -4,6 +4,8 @@
 // material_properties.cpp, include/MIDSX/Core/material_helpers.h:110-121.
 #include <dlfcn.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <random>
 #include <stdexcept>
@@ -54,6 +56,36 @@ double MaterialData::eval(int which, double x) const {
     double y = 0;
     midsx::check(midsx_tables_eval(blob_->blob, index_, which, &x, &y, 1), "midsx_tables_eval");
     return y;
+}
+
+double MaterialData::interpolateMassEnergyAbsorptionCoefficient(double energy) const {
+    if (!mu_en_table_.empty()) {
+        // LogLogLinear clamped at the table's ends (src/MIDSX/Core/interpolators.cpp:33-76)
+        const auto& t = mu_en_table_;
+        const double lx = std::log10(energy);
+        if (lx <= std::log10(t.front().first)) return t.front().second;
+        if (lx >= std::log10(t.back().first)) return t.back().second;
+        const size_t j = size_t(std::upper_bound(t.begin(), t.end(), energy,
+                                                 [](double v, const std::pair<double, double>& p) {
+                                                     return v < p.first;
+                                                 }) -
+                                t.begin());
+        const double x1 = std::log10(t[j - 1].first), x2 = std::log10(t[j].first);
+        const double y1 = std::log10(t[j - 1].second), y2 = std::log10(t[j].second);
+        return std::pow(10.0, y1 + (y2 - y1) / (x2 - x1) * (lx - x1));
+    }
+    double y = 0;
+    midsx::check(midsx_tables_mu_en(blob_->blob, index_, &energy, &y, 1), "midsx_tables_mu_en");
+    return y;
+}
+
+void MaterialData::setMassEnergyAbsorptionCoefficients(std::vector<std::pair<double, double>> table) {
+    if (table.size() < 2) throw std::invalid_argument("a mu_en/rho table needs at least two nodes");
+    for (size_t i = 0; i < table.size(); ++i) {
+        if (!(table[i].first > 0) || !(table[i].second > 0) || (i && !(table[i].first > table[i - 1].first)))
+            throw std::invalid_argument("mu_en/rho table: positive values at ascending energies");
+    }
+    mu_en_table_ = std::move(table);
 }
 
 double MaterialData::sampleCoherentScatteringDCS(double energy) const {

@@ -188,6 +188,20 @@ SurfaceQuantityContainer SurfaceQuantityContainer::operator+(SurfaceQuantityCont
         r.addVectorQuantity(a + o.vector_.at(v.first));
     }
     for (auto& c : count_) r.addCountQuantity(c.second + o.count_.at(c.first));
+    if (spectrum_.empty()) {
+        r.spectrum_ = o.spectrum_;
+    } else if (o.spectrum_.empty()) {
+        r.spectrum_ = spectrum_;
+    } else {
+        if (spectrum_.n != o.spectrum_.n || spectrum_.e_min != o.spectrum_.e_min ||
+            spectrum_.e_width != o.spectrum_.e_width)
+            throw std::runtime_error("Cannot add SurfaceQuantityContainers with different energy spectra.");
+        r.spectrum_ = spectrum_;
+        for (size_t i = 0; i < r.spectrum_.count.size(); ++i) {
+            r.spectrum_.count[i] += o.spectrum_.count[i];
+            r.spectrum_.cosine[i] += o.spectrum_.cosine[i];
+        }
+    }
     return r;
 }
 
@@ -251,6 +265,20 @@ midsx_tally_spec SurfaceTally::describe() const {
     throw std::invalid_argument("this SurfaceTally type has no GPU implementation");
 }
 
+void SurfaceTally::setEnergyBins(double e_min, double e_width, int n) {
+    if (n < 1 || n > MIDSX_MAX_ENERGY_BINS || !(e_width > 0) || !std::isfinite(e_min) || !std::isfinite(e_width))
+        throw std::invalid_argument("energy bins need 1 <= n <= MIDSX_MAX_ENERGY_BINS and e_width > 0");
+    e_min_ = e_min;
+    e_width_ = e_width;
+    n_energy_ = n;
+}
+
+void SurfaceTally::describeSpectrum(midsx_tally_spec& s) const {
+    s.n_energy = n_energy_;
+    s.e_min = e_min_;
+    s.e_width = e_width_;
+}
+
 DiscSurfaceTally::DiscSurfaceTally(Vec3 center, Vec3 norm, double radius, const SurfaceQuantityContainer& quantities)
     : center_(center), radius_(radius) {
     surface_quantities_ = quantities;
@@ -264,6 +292,7 @@ midsx_tally_spec DiscSurfaceTally::describe() const {
     put(s.a, center_);
     put(s.b, norm_);
     s.radius = radius_;
+    describeSpectrum(s);
     return s;
 }
 
@@ -282,6 +311,7 @@ midsx_tally_spec RectangularSurfaceTally::describe() const {
     put(s.a, corner_);
     put(s.b, edge1_);
     put(s.c, edge2_);
+    describeSpectrum(s);
     return s;
 }
 
@@ -297,5 +327,7 @@ midsx_tally_spec BinnedRectangularSurfaceTally::describe() const {
     s.kind = MIDSX_TALLY_SURFACE_BINNED_RECT;
     s.nu = nu_;
     s.nv = nv_;
+    if (n_energy_ > 0) throw std::invalid_argument("a binned surface tally keeps no energy spectrum");
+    s.n_energy = 0;
     return s;
 }

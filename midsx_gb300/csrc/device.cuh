@@ -422,16 +422,18 @@ MIDSX_HD bool rita_sample(const DevTables& t, const DevRita& T, R E, R y, R& mu)
 
 // -------------------------------------------------------------------- tally specs ---
 struct DevTally {
-    int kind, nu, nv, reserved;
+    int kind, nu, nv, n_energy;  // n_energy: incident-energy spectrum bins of a DISC / RECT
     double a[3], b[3], c[3];
     double radius;
     double norm[3];      // plane normal used for the entrance cosine
     double e1e1, e2e2;   // rectangle basis dot products
+    double e_min, e_width;  // spectrum bins [e_min + k e_width, e_min + (k+1) e_width)
     unsigned long long* acc;
     // FP32 copies for the mixed form
     float fa[3], fb[3], fc[3], fnorm[3];
-    float fradius, fe1e1, fe2e2;
+    float fradius, fe1e1, fe2e2, fe_min, fe_width;
 };
+
 
 // The working-precision value of a field stored in FP64 with an FP32 copy.
 template <typename R>
@@ -440,6 +442,15 @@ MIDSX_HD R pickr(double d, float f) {
         return d;
     else
         return f;
+}
+
+// Spectrum bin of incident energy E, -1 outside the tally's n_energy bins: floor((E - e_min) /
+// e_width) in the working precision (IEEE division, as the oracle computes it in FP64).
+template <typename R>
+__device__ __forceinline__ int energy_bin(const DevTally& T, R E) {
+    const R k = (E - pickr<R>(T.e_min, T.fe_min)) / pickr<R>(T.e_width, T.fe_width);
+    if (!(k >= R(0)) || k >= R(T.n_energy)) return -1;
+    return int(k);
 }
 
 // fixed-point scales of the mixed path (per eV, per eV^2, per unit cosine)

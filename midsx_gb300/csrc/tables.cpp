@@ -789,6 +789,61 @@ extern "C" midsx_status midsx_tables_eval(const midsx_table_blob* blob, int32_t 
     return MIDSX_OK;
 }
 
+namespace {
+
+// Mean fraction of the photon energy given to the electron in one incoherent scatter at
+// k = E / mec2, under the transport's sampling density KN(mu) * S(alpha k sqrt(1 - mu))
+// (photon_interactions.cpp:62-141).  Substituting t = sqrt(1 - mu) makes the S(x) argument
+// linear in t; composite 8-point Gauss-Legendre over 256 panels of t in [0, sqrt 2].
+double incoherent_transfer_fraction(const double* D, const midsx_lin_table& sf, double k) {
+    static const double gx[8] = {-0.9602898564975363, -0.7966664774136267, -0.5255324099163290,
+                                 -0.1834346424956498, 0.1834346424956498,  0.5255324099163290,
+                                 0.7966664774136267,  0.9602898564975363};
+    static const double gw[8] = {0.1012285362903763, 0.2223810344533745, 0.3137066678687174,
+                                 0.3626837833783620, 0.3626837833783620, 0.3137066678687174,
+                                 0.2223810344533745, 0.1012285362903763};
+    const int panels = 256;
+    const double t_hi = std::sqrt(2.0), h = t_hi / panels;
+    const double alpha = midsx::alpha_inv_angstrom();
+    double num = 0, den = 0;
+    for (int p = 0; p < panels; ++p) {
+        const double c = (p + 0.5) * h;
+        for (int q = 0; q < 8; ++q) {
+            const double t = c + 0.5 * h * gx[q];
+            const double mu = 1 - t * t;
+            const double r = 1 / (1 + k * (1 - mu));  // k'/k
+            const double kn = r * r * (r + 1 / r - (1 - mu * mu));
+            const double s = midsx::lin_eval(D + sf.x, D + sf.lx, D + sf.ly, sf.n, alpha * k * t);
+            const double w = gw[q] * 2 * t * kn * s;  // d(mu) = 2 t dt
+            num += w * (1 - r);
+            den += w;
+        }
+    }
+    return den > 0 ? num / den : 0.0;
+}
+
+}  // namespace
+
+extern "C" midsx_status midsx_tables_mu_en(const midsx_table_blob* blob, int32_t material, const double* x,
+                                           double* y, int64_t n) {
+    if (!blob || !x || !y || n < 0 || material < 0 || material >= blob->n_materials) return MIDSX_INVALID_ARG;
+    const double* D = blob->data;
+    const midsx_material_table& m = blob->mat[material];
+    if (!(m.density > 0)) return MIDSX_INVALID_ARG;
+    for (int64_t i = 0; i < n; ++i) {
+        const double E = x[i];
+        if (!(E > 0) || E > blob->e_max) return MIDSX_TABLE_RANGE;
+        const double photo = midsx::lin_eval(D + m.photo.x, D + m.photo.lx, D + m.photo.ly, m.photo.n, E);
+        const midsx_spline_table& st = m.incoh;
+        const int span = midsx::spline_span(D + st.knot_e, st.n_ctrl, st.degree, E);
+        const double incoh = midsx::spline_eval_at(D + st.knot_u, D + st.ctrl, st.degree, span, st.lx_min,
+                                                   st.lx_max, E);
+        const double f = incoherent_transfer_fraction(D, m.sfunc, E / midsx::kElectronRestMass);
+        y[i] = (photo + incoh * f) / m.density;
+    }
+    return MIDSX_OK;
+}
+
 extern "C" const char* midsx_status_string(midsx_status s) {
     switch (s) {
         case MIDSX_OK: return "ok";

@@ -266,6 +266,16 @@ __device__ __forceinline__ void score_tallies(const DevTally* tallies, int n_tal
         vec_cosine<R, MX>(acc, 1, cls0, ec, words);
         count1(acc + 24 + cls0);
         ++words;
+        if (T.n_energy > 0) {
+            // incident-energy spectrum: [crossings, entrance-cosine sum] per bin and class
+            const int kb = energy_bin<R>(T, E);
+            if (kb >= 0) {
+                unsigned long long* sp = acc + MIDSX_SCALAR_SLOTS + (size_t(kb) * 4 + cls0) * 2;
+                count1(sp);
+                Acc<MX>::cosine(sp + 1, ec);
+                ++words;
+            }
+        }
     }
 }
 
@@ -993,6 +1003,15 @@ midsx_status tallies_layout(size_t n_voxels, const midsx_tally_spec* specs, int3
         d.kind = s.kind;
         d.nu = s.nu;
         d.nv = s.nv;
+        d.n_energy = s.n_energy;
+        d.e_min = s.e_min;
+        d.e_width = s.e_width;
+        const bool scalar_surface = s.kind == MIDSX_TALLY_SURFACE_DISC || s.kind == MIDSX_TALLY_SURFACE_RECT;
+        if (s.n_energy < 0 || s.n_energy > MIDSX_MAX_ENERGY_BINS || (s.n_energy > 0 && !scalar_surface) ||
+            (s.n_energy > 0 && !(s.e_width > 0.0 && std::isfinite(s.e_width) && std::isfinite(s.e_min)))) {
+            set_last_error("energy spectrum: DISC or RECT tally, 0 < n_energy <= MIDSX_MAX_ENERGY_BINS, e_width > 0");
+            return MIDSX_INVALID_ARG;
+        }
         for (int k = 0; k < 3; ++k) {
             d.a[k] = s.a[k];
             d.b[k] = s.b[k];
@@ -1030,8 +1049,12 @@ midsx_status tallies_layout(size_t n_voxels, const midsx_tally_spec* specs, int3
         d.fradius = float(d.radius);
         d.fe1e1 = float(d.e1e1);
         d.fe2e2 = float(d.e2e2);
+        d.fe_min = float(d.e_min);
+        d.fe_width = float(d.e_width);
         d.acc = reinterpret_cast<unsigned long long*>(words);  // offset, fixed after allocation
-        words += (s.kind == MIDSX_TALLY_SURFACE_BINNED_RECT) ? size_t(s.nu) * s.nv * 8 : kScalarWords;
+        // a spectrum follows the scalar words: [bin][class][crossings, cosine sum]
+        words += (s.kind == MIDSX_TALLY_SURFACE_BINNED_RECT) ? size_t(s.nu) * s.nv * 8
+                                                              : kScalarWords + size_t(d.n_energy) * 8;
         t->host_specs.push_back(d);
     }
     t->acc_words = words;
@@ -1401,6 +1424,30 @@ extern "C" midsx_status midsx_gpu_fetch_binned(midsx_tallies_h t, int32_t index,
             }
         }
         if (count) count[i] = double(h[2 * i + 1]);
+    }
+    return MIDSX_OK;
+}
+
+extern "C" midsx_status midsx_gpu_fetch_spectrum(midsx_tallies_h t, int32_t index, double* count, double* cosine,
+                                                 void* stream) {
+    if (!t || index < 0 || index >= int32_t(t->host_specs.size())) return MIDSX_INVALID_ARG;
+    const DevTally& d = t->host_specs[index];
+    if (d.n_energy <= 0) return MIDSX_INVALID_ARG;
+    const size_t cells = size_t(d.n_energy) * 4;
+    std::vector<unsigned long long> h(cells * 2);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), d.acc + kScalarWords, h.size() * 8, cudaMemcpyDeviceToHost,
+                             static_cast<cudaStream_t>(stream)));
+    midsx_status st = wait_stream(stream);
+    if (st != MIDSX_OK) return st;
+    const bool mixed = t->precision == MIDSX_PREC_MIXED;
+    for (size_t i = 0; i < cells; ++i) {
+        if (count) count[i] = double(h[2 * i]);
+        if (cosine) {
+            if (mixed)
+                cosine[i] = fx_signed(h[2 * i + 1], kFxCosine);
+            else
+                std::memcpy(&cosine[i], &h[2 * i + 1], 8);
+        }
     }
     return MIDSX_OK;
 }

@@ -12,6 +12,7 @@ from . import build as _build
 
 MAX_MATERIALS = 16
 SCALAR_SLOTS = 40
+MAX_ENERGY_BINS = 65536
 
 OK, INVALID_ARG, OOM, TIMEOUT, STEP_CAP, TABLE_RANGE, CUDA_ERROR, NOT_FOUND, IO_ERROR = range(9)
 PREC_FP64, PREC_MIXED = 0, 1
@@ -75,8 +76,8 @@ class SourceSpec(C.Structure):
 
 class TallySpec(C.Structure):
     _fields_ = [("kind", C.c_int32), ("nu", C.c_int32), ("nv", C.c_int32),
-                ("reserved", C.c_int32), ("a", D3), ("b", D3), ("c", D3),
-                ("radius", C.c_double)]
+                ("n_energy", C.c_int32), ("a", D3), ("b", D3), ("c", D3),
+                ("radius", C.c_double), ("e_min", C.c_double), ("e_width", C.c_double)]
 
 
 class RunConfig(C.Structure):
@@ -150,6 +151,7 @@ _SIGNATURES = {
     "midsx_catalog_id": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_int32)]),
     "midsx_catalog_name": (C.c_int, [C.c_char_p, C.c_int32, C.c_char_p, C.c_int32]),
     "midsx_tables_eval": (C.c_int, [C.POINTER(TableBlob), C.c_int32, C.c_int32, PD, PD, C.c_int64]),
+    "midsx_tables_mu_en": (C.c_int, [C.POINTER(TableBlob), C.c_int32, PD, PD, C.c_int64]),
     "midsx_status_string": (C.c_char_p, [C.c_int]),
     "midsx_last_error": (C.c_char_p, []),
     "midsx_gpu_tables_create": (C.c_int, [C.POINTER(TableBlob), C.POINTER(VP)]),
@@ -168,6 +170,7 @@ _SIGNATURES = {
     "midsx_gpu_fetch_dose": (C.c_int, [VP, PD, PD, PD, VP]),
     "midsx_gpu_fetch_scalar": (C.c_int, [VP, C.c_int32, PD, VP]),
     "midsx_gpu_fetch_binned": (C.c_int, [VP, C.c_int32, PD, PD, VP]),
+    "midsx_gpu_fetch_spectrum": (C.c_int, [VP, C.c_int32, PD, PD, VP]),
     "midsx_gpu_run_host": (C.c_int, [VP, C.POINTER(GeometrySpec), C.c_void_p, C.POINTER(SourceSpec),
                                      C.POINTER(TallySpec), C.c_int32, C.c_int32, C.POINTER(RunConfig),
                                      PD, C.POINTER(RunStats)]),

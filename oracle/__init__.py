@@ -25,7 +25,9 @@ PD = C.POINTER(C.c_double)
 class OracleResult(C.Structure):
     _fields_ = [("dose_sum", PD), ("dose_sumsq", PD), ("dose_count", PD), ("scalar", PD),
                 ("binned_energy", PD), ("binned_count", PD), ("history_deposit", PD),
-                ("stats", N.RunStats), ("run_time", C.c_double)]
+                ("stats", N.RunStats), ("run_time", C.c_double),
+                ("spectrum_count", PD), ("spectrum_cosine", PD), ("raw_spec", C.c_int32), ("reserved", C.c_int32),
+                ("raw_cap", C.c_int64), ("raw_energy", PD), ("raw_cosine", PD), ("raw_n", C.c_int64)]
 
 
 _lib = None
@@ -60,11 +62,12 @@ def load():
 
 
 def run(blob, domain, spacing, origin, ids, background_id, source, specs=(), n=1000, seed=1, first=0,
-        rng=RNG_PHILOX, threads=0, max_steps=0, max_trials=0, dose=True, history=False, grids=None):
+        rng=RNG_PHILOX, threads=0, max_steps=0, max_trials=0, dose=True, history=False, grids=None, raw_spec=None):
     """blob: midsx_gb300.TableBlob; ids shaped (nz, ny, nx); source: dict(position, direction,
     energy|spectrum) as for midsx_gb300.source_spec; specs: tally dicts.  grids: optional list
     of (ids, spacing, origin) for a domain of several grids (then spacing, origin and ids are
-    ignored and dose arrays come as one list entry per grid)."""
+    ignored and dose arrays come as one list entry per grid).  raw_spec: index of a surface
+    tally whose raw primary IncidentEnergy / EntranceCosine vectors are returned (out["raw"])."""
     lib = load()
     shapes = None
     if grids is not None:
@@ -102,6 +105,20 @@ def run(blob, domain, spacing, origin, ids, background_id, source, specs=(), n=1
     if history:
         keep["history_deposit"] = np.zeros(int(n))
         res.history_deposit = N.dptr(keep["history_deposit"])
+    ns = sum(int(d["spectrum"][2]) * 4 for d in specs if d.get("spectrum") is not None)
+    keep["spectrum_count"] = np.zeros(max(1, ns))
+    keep["spectrum_cosine"] = np.zeros(max(1, ns))
+    res.spectrum_count = N.dptr(keep["spectrum_count"])
+    res.spectrum_cosine = N.dptr(keep["spectrum_cosine"])
+    res.raw_spec = -1 if raw_spec is None else int(raw_spec)
+    if raw_spec is not None:
+        # a primary crosses a plane once per history (a straight line, one direction; twice
+        # only if the crossing falls exactly on a step boundary)
+        keep["raw_energy"] = np.zeros(2 * int(n))
+        keep["raw_cosine"] = np.zeros(2 * int(n))
+        res.raw_cap = 2 * int(n)
+        res.raw_energy = N.dptr(keep["raw_energy"])
+        res.raw_cosine = N.dptr(keep["raw_cosine"])
     if grids is not None:
         dom = (C.c_double * 3)(*[float(x) for x in domain])
         rc = lib.oracle_run_grids(blob.ptr, dom, int(background_id), garr, len(grids), C.byref(s), arr, len(specs),
@@ -139,6 +156,18 @@ def run(blob, domain, spacing, origin, ids, background_id, source, specs=(), n=1
         else:
             binned.append(None)
     out["binned"] = binned
+    spectra, off = [], 0
+    for d in specs:
+        if d.get("spectrum") is not None:
+            k = int(d["spectrum"][2]) * 4
+            spectra.append((keep["spectrum_count"][off:off + k].reshape(-1, 4),
+                            keep["spectrum_cosine"][off:off + k].reshape(-1, 4)))
+            off += k
+        else:
+            spectra.append(None)
+    out["spectrum"] = spectra
+    if raw_spec is not None:
+        out["raw"] = (keep["raw_energy"][:res.raw_n].copy(), keep["raw_cosine"][:res.raw_n].copy())
     if history:
         out["history_deposit"] = keep["history_deposit"]
     return out

@@ -730,6 +730,19 @@ typedef struct oracle_result {
     double* history_deposit;/* n histories: energy deposited in grid voxels, or NULL */
     midsx_run_stats stats;
     double run_time;        /* seconds in the history loop (the reference's run_time) */
+    /* incident-energy spectra of the DISC / RECT specs with n_energy > 0, binned from the
+     * raw IncidentEnergy / EntranceCosine vectors: [bin][class] crossings and cosine sums,
+     * specs in order, or NULL */
+    double* spectrum_count;
+    double* spectrum_cosine;
+    /* the raw primary IncidentEnergy and EntranceCosine vectors of surface spec raw_spec
+     * (-1: none), up to raw_cap values each; raw_n receives the number of values */
+    int32_t raw_spec;
+    int32_t reserved;
+    int64_t raw_cap;
+    double* raw_energy;
+    double* raw_cosine;
+    int64_t raw_n;
 } oracle_result;
 
 }  // extern "C"
@@ -949,6 +962,45 @@ int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size
         if (out->dose_sum) std::memcpy(out->dose_sum, s.data(), nvox * 8);
         if (out->dose_sumsq) std::memcpy(out->dose_sumsq, s2.data(), nvox * 8);
         if (out->dose_count) std::memcpy(out->dose_count, c.data(), nvox * 8);
+    }
+    // spectra: every raw (IncidentEnergy, EntranceCosine) pair binned by energy; both values
+    // of a crossing are non-zero, so the two vectors of a class run in step
+    size_t soff = 0;
+    for (int i = 0; i < n_specs; ++i) {
+        const midsx_tally_spec& sp = specs[i];
+        if (sp.n_energy <= 0) continue;
+        const size_t cells = size_t(sp.n_energy) * 4;
+        std::vector<double> cnt(cells, 0.0), cs(cells, 0.0);
+        for (auto& st : states) {
+            TallyReplica& r = st.tallies[size_t(i)];
+            for (int c = 0; c < 4; ++c) {
+                const auto& ev = r.vec[0][c].values;
+                const auto& cv = r.vec[1][c].values;
+                for (size_t k = 0; k < ev.size() && k < cv.size(); ++k) {
+                    const double b = (ev[k] - sp.e_min) / sp.e_width;
+                    if (!(b >= 0) || b >= double(sp.n_energy)) continue;
+                    const size_t cell = size_t(int(b)) * 4 + size_t(c);
+                    cnt[cell] += 1;
+                    cs[cell] += cv[k];
+                }
+            }
+        }
+        if (out->spectrum_count) std::memcpy(out->spectrum_count + soff, cnt.data(), cells * 8);
+        if (out->spectrum_cosine) std::memcpy(out->spectrum_cosine + soff, cs.data(), cells * 8);
+        soff += cells;
+    }
+    out->raw_n = 0;
+    if (out->raw_spec >= 0 && out->raw_spec < n_specs) {
+        for (auto& st : states) {
+            TallyReplica& r = st.tallies[size_t(out->raw_spec)];
+            const auto& ev = r.vec[0][0].values;
+            const auto& cv = r.vec[1][0].values;
+            for (size_t k = 0; k < ev.size() && k < cv.size() && out->raw_n < out->raw_cap; ++k) {
+                if (out->raw_energy) out->raw_energy[out->raw_n] = ev[k];
+                if (out->raw_cosine) out->raw_cosine[out->raw_n] = cv[k];
+                out->raw_n++;
+            }
+        }
     }
     size_t boff = 0;
     for (int i = 0; i < n_specs; ++i) {

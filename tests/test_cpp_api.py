@@ -185,3 +185,41 @@ def test_cpp_multi_grid_program_equals_python_api(tmp_path):
     for k in range(3):
         assert float(out["grid_deposit"][k][1]) == pytest.approx(dose[k].sum(), rel=1e-12), k
     assert dose[0].sum() > 0 and dose[2].sum() > 0
+
+
+@pytest.mark.gpu
+def test_cpp_spectrum_air_kerma_program(golden, tmp_path):
+    """The reference's hvl_30kVp.cpp form: a polyenergetic source read from a spectrum CSV
+    and DerivedQuantity::getPrimarySpectrumAirKerma over the spectrum files' midpoints.  The
+    engine's default spectrum bins (one per source line) give the air kerma that the Python
+    API computes on the same Philox streams, and the reference's AK_hvl / AK_0."""
+    from midsx_gb300 import derived as D
+    from midsx_gb300 import native as N
+    from midsx_gb300 import scenes
+    sp = np.array(golden["spectra"][golden["spectrum_of_case"]["30kVp"]])
+    csv = tmp_path / "spectrum.csv"
+    csv.write_text("".join("%r,%r\n" % (float(e), float(w)) for e, w in sp))
+    n = 1_000_000
+    air = run_hvl(["-", str(csv), n])
+    s = golden["cases"]["30kVp"]["slab_hvl"]
+    hvl = run_hvl(["-", str(csv), n, s["dims"][2], s["spacing_cm"][2]])
+    # the air-only run through the Python API: tables of air alone, as the C++ domain has
+    sc = golden["scene"]
+    tables = M.Tables([scenes.AIR], e_max=150e3)
+    ph = M.Phantom(tables, sc["domain"], (4, 4, 1e-4), sc["slab_origin"], np.full((1, 1, 1), scenes.AIR, np.uint8),
+                   scenes.AIR)
+    src = dict(position=sc["source"]["position"],
+               direction=("disc", sc["source"]["disc_center"], sc["source"]["disc_normal"],
+                          sc["source"]["disc_radius"]),
+               spectrum=(sp[:, 0] * 1e3, sp[:, 1]))
+    tally = dict(kind="disc", spectrum=D.source_bins(src), **sc["disc_tally"])
+    tl = M.Tallies(ph, [tally], N.DOSE_OFF)
+    M.run(tables, ph, M.Source(**src), tl, n, seed=1, first=0, precision="mixed")
+    midpoints = [(0.25 + 0.5 * k) * 1e3 for k in range(239)]
+    assert D.primary_spectrum_air_kerma(tl, 0, tables, midpoints) == pytest.approx(air["primary_air_kerma"], rel=1e-12)
+    r = hvl["primary_air_kerma"] / air["primary_air_kerma"]
+    ref = golden["cases"]["30kVp"]["AK_hvl"]["mean"] / golden["cases"]["30kVp"]["AK_0"]["mean"]
+    pa, pb = hvl["primary_photons"] / n, air["primary_photons"] / n
+    sig = r * math.sqrt((1 - pa) / (n * pa) + (1 - pb) / (n * pb))
+    # 0.5 %: the allowance for the two builds' cross-section tables (test_derived.POLY_SYSTEMATIC)
+    assert abs(r - ref) < 4 * sig + 0.005 * ref, (r, ref, sig)
