@@ -306,7 +306,9 @@ def main():
     if "e2e" not in result:
         result["e2e"] = None
     if not args.quick:
-        result["background_fast_tracking"] = fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, N_hist)
+        for mode in ("background_fast", "macro_cell"):
+            result[mode + "_tracking"] = fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, N_hist,
+                                                           mode)
     if not args.quick and args.radiography:
         result["radiography_precision_ablation"] = radiography_leg(args, np, torch)
     if not args.quick and args.batched:
@@ -316,9 +318,10 @@ def main():
     print(json.dumps(result), flush=True)
 
 
-def fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, n_hist):
+def fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, n_hist, mode):
     """The same workload with MIDSX_TRACK_BACKGROUND_FAST (flights in the background air use
-    the air's own attenuation and stop at the grid): not the reference's algorithm, so it is
+    the air's own attenuation and stop at the grid) or MIDSX_TRACK_MACRO_CELL (also local
+    majorants of 8^3-voxel cells inside the grid): not the reference's algorithm, so it is
     reported beside the headline, with its dose checked statistically against the reference
     algorithm on 2e6 histories."""
     stream = torch.cuda.current_stream()
@@ -329,7 +332,7 @@ def fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, n_hist):
         tl.reset(sptr)
         ev[0].record(stream)
         M.run(tables, ph, src, tl, n_hist, seed=11, first=(50 + i) * n_hist, precision="mixed", stream=sptr,
-              tracking="background_fast")
+              tracking=mode)
         ev[1].record(stream)
         torch.cuda.synchronize()
         if i:
@@ -337,12 +340,12 @@ def fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, n_hist):
     st = tl.stats()
     ncmp = 2_000_000
     doses = {}
-    for mode in ("reference", "background_fast"):
+    for m in ("reference", mode):
         tl.reset(sptr)
-        M.run(tables, ph, src, tl, ncmp, seed=91 if mode == "reference" else 92, precision="mixed", stream=sptr,
-              tracking=mode)
-        doses[mode] = tl.dose(sptr)
-    a, b = doses["reference"], doses["background_fast"]
+        M.run(tables, ph, src, tl, ncmp, seed=91 if m == "reference" else 92, precision="mixed", stream=sptr,
+              tracking=m)
+        doses[m] = tl.dose(sptr)
+    a, b = doses["reference"], doses[mode]
     s1, q1, s2, q2 = (x.ravel() for x in (a["sum"], a["sumsq"], b["sum"], b["sumsq"]))
     sel = (s1 + s2) > 0.01 * max(s1.max(), s2.max())
     z = (s1[sel] - s2[sel]) / np.sqrt(q1[sel] + q2[sel])
@@ -393,8 +396,16 @@ def radiography_leg(args, np, torch):
     scat_a, scat_b = a[..., 1:].sum(axis=2).ravel(), b[..., 1:].sum(axis=2).ravel()
     hit = prim_b > 0
     rel = np.abs(prim_a[hit] - prim_b[hit]) / prim_b[hit]
-    fast_dt = timed(n, "mixed", tracking="background_fast", seed=6)
-    fst = tl.stats(sptr)
+    opt_in = {}
+    for mode, seed in (("background_fast", 6), ("macro_cell", 7)):
+        dt = timed(n, "mixed", tracking=mode, seed=seed)
+        st = tl.stats(sptr)
+        e, c = tl.binned(0, sptr)
+        p = e[..., 0].ravel()
+        opt_in[mode] = {"value": n / dt, "unit": UNIT, "steps_per_history": st["steps"] / st["histories"],
+                        "primary_total_rel_diff_vs_reference": float(abs(p.sum() - prim_a.sum()) / prim_a.sum()),
+                        "scatter_total_rel_diff_vs_reference":
+                            float(abs(e[..., 1:].sum() - scat_a.sum()) / scat_a.sum())}
     return {"workload": sc.name + " (512^2 detector at 100 cm SID, 16 Pb spheres)", "histories": n,
             "mixed": out["mixed"], "fp64": out["fp64"], "mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"],
             "identical_streams": {
@@ -402,8 +413,7 @@ def radiography_leg(args, np, torch):
                 "scatter_total_rel_diff": float(abs(scat_a.sum() - scat_b.sum()) / scat_b.sum()),
                 "primary_bins_identical": float(np.mean(prim_a[hit] == prim_b[hit])) if hit.any() else None,
                 "primary_bins_rel_diff_p99": float(np.percentile(rel, 99)) if hit.any() else None},
-            "background_fast_tracking": {"value": n / fast_dt, "unit": UNIT,
-                                         "steps_per_history": fst["steps"] / fst["histories"]}}
+            "opt_in_tracking": opt_in}
 
 
 def batched_leg(args, torch):

@@ -197,6 +197,11 @@ typedef struct midsx_grid_spec {
 midsx_status midsx_gpu_phantom_create_grids(midsx_tables_h tables, const double* domain, int32_t background_id,
                                             const midsx_grid_spec* grids, int32_t n_grids, midsx_phantom_h* out);
 
+/* Rebuilds the phantom's macro cells (MIDSX_TRACK_MACRO_CELL) with edges of `edge` voxels, a
+ * power of two in [1, 64]; the phantom is created with MIDSX_MACRO_CELL.  Synchronous; no run
+ * may use the phantom meanwhile. */
+midsx_status midsx_gpu_phantom_macro_cells(midsx_phantom_h p, int32_t edge);
+
 /* PhotonSource (src/MIDSX/Core/source.cpp:44-155).  Geometry is a point (PointGeometry).
  * Directionality:
  *   BEAM:        a = pass-through point
@@ -293,8 +298,19 @@ typedef enum midsx_scheduler {
  * with REFERENCE statistically, not history by history.  Photon-pool scheduler only. */
 typedef enum midsx_tracking {
     MIDSX_TRACK_REFERENCE = 0,
-    MIDSX_TRACK_BACKGROUND_FAST = 1
+    MIDSX_TRACK_BACKGROUND_FAST = 1,
+    MIDSX_TRACK_MACRO_CELL = 2
 } midsx_tracking;
+/* MACRO_CELL adds local majorants inside the grids to BACKGROUND_FAST: every grid is split
+ * into cells of MIDSX_MACRO_CELL^3 voxels (midsx_gpu_phantom_macro_cells changes the edge),
+ * each with the set of materials it holds (built with the phantom).  A flight inside a grid draws one optical depth -ln U and spends it cell
+ * by cell along the ray, each cell's majorant being the largest attenuation among its own
+ * materials at the photon's energy; where the depth runs out a voxel is fetched and the
+ * collision is real with probability mu(voxel) / mu(cell).  A flight that leaves its grid
+ * ends on the grid's face.  Unbiased, statistically equal to REFERENCE; photon pool only.
+ * Where grids overlap, the cells of a later grid that meet an earlier grid's box take every
+ * material of the tables (the first grid owns the overlap). */
+#define MIDSX_MACRO_CELL 8
 
 typedef struct midsx_run_config {
     int32_t precision;           /* midsx_precision */

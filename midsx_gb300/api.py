@@ -175,6 +175,11 @@ class Phantom:
     def n_voxels(self):
         return int(sum(np.prod(sh) for sh in self.grid_shapes))
 
+    def macro_cells(self, edge):
+        """Rebuilds the macro cells of MIDSX_TRACK_MACRO_CELL with edges of `edge` voxels (a
+        power of two, 1..64; the phantom starts with 8)."""
+        N.check(N.load().midsx_gpu_phantom_macro_cells(self.handle, int(edge)), "midsx_gpu_phantom_macro_cells")
+
     def close(self):
         if self.handle:
             N.load().midsx_gpu_phantom_destroy(self.handle)
@@ -361,7 +366,8 @@ PRECISIONS = {"fp64": N.PREC_FP64, "mixed": N.PREC_MIXED}
 SCHEDULERS = {"default": N.SCHED_DEFAULT, "lanes": N.SCHED_LANES, "pool": N.SCHED_POOL}
 
 
-TRACKING = {"reference": N.TRACK_REFERENCE, "background_fast": N.TRACK_BACKGROUND_FAST}
+TRACKING = {"reference": N.TRACK_REFERENCE, "background_fast": N.TRACK_BACKGROUND_FAST,
+            "macro_cell": N.TRACK_MACRO_CELL}
 
 
 def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0, regroup=0,

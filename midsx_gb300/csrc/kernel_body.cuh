@@ -120,6 +120,9 @@ struct Geo {
     const uint8_t* ids;
     int n_grids;           // grids of the domain; the first is held above
     const DevGrid* extra;  // the others, in first-hit order
+    const uint32_t* cells; // macro-cell material masks (every grid)
+    int cnx, cny, cnz;     // macro cells of the first grid
+    int cshift;            // macro-cell edge = 2^cshift voxels
 };
 
 template <typename R>
@@ -137,13 +140,19 @@ __device__ Geo<R> make_geo(const DevGeom& G) {
     g.ids = G.ids;
     g.n_grids = G.n_grids;
     g.extra = G.extra;
+    g.cells = G.cells;
+    g.cnx = G.cdims[0];
+    g.cny = G.cdims[1];
+    g.cnz = G.cdims[2];
+    g.cshift = G.cell_shift;
     return g;
 }
 
 // Distance along the ray p + t d (t >= 0) to the closed box [lo, lo + ext], +inf if the ray
-// misses it (slab method); 0 if p is inside.
+// misses it (slab method) or meets it for no more than `tol` (grazing it, or leaving it from
+// a point within tol of its far side); 0 if p is inside.
 template <typename R>
-__device__ __forceinline__ R box_entry(const V3<R>& p, const V3<R>& d, const V3<R>& lo, const V3<R>& ext) {
+__device__ __forceinline__ R box_entry(const V3<R>& p, const V3<R>& d, const V3<R>& lo, const V3<R>& ext, R tol) {
     R tmin = R(0), tmax = R(INFINITY);
     const R pp[3] = {p.x, p.y, p.z}, dd[3] = {d.x, d.y, d.z}, ll[3] = {lo.x, lo.y, lo.z}, ee[3] = {ext.x, ext.y, ext.z};
 #pragma unroll
@@ -161,13 +170,22 @@ __device__ __forceinline__ R box_entry(const V3<R>& p, const V3<R>& d, const V3<
         tmin = t1 > tmin ? t1 : tmin;
         tmax = t2 < tmax ? t2 : tmax;
     }
-    return tmin <= tmax ? tmin : R(INFINITY);
+    return tmax > tmin + tol ? tmin : R(INFINITY);
+}
+
+// The rounding allowance of a grid's faces: 1e-4 of its smallest voxel edge.
+template <typename R>
+__device__ __forceinline__ R face_tol(const V3<R>& spc) {
+    const R m = spc.x < spc.y ? spc.x : spc.y;
+    return R(1e-4) * (m < spc.z ? m : spc.z);
 }
 
 // Distance along a ray from the background to the first grid box it enters, +inf if none.
+// A grid the ray only grazes, or leaves from a point within the rounding allowance of its
+// face (where a macro-cell flight ends), is not entered.
 template <typename R, bool MX>
 __device__ __forceinline__ R grid_entry(const Geo<R>& g, const V3<R>& p, const V3<R>& d) {
-    R best = box_entry<R>(p, d, g.org, g.ext);
+    R best = box_entry<R>(p, d, g.org, g.ext, face_tol<R>(g.spc));
     for (int k = 0; k + 1 < g.n_grids; ++k) {
         const DevGrid& G = g.extra[k];
         V3<R> o, e;
@@ -178,10 +196,149 @@ __device__ __forceinline__ R grid_entry(const Geo<R>& g, const V3<R>& p, const V
             o = {G.origin[0], G.origin[1], G.origin[2]};
             e = {G.ext[0], G.ext[1], G.ext[2]};
         }
-        const R t = box_entry<R>(p, d, o, e);
+        const V3<R> sp = {R(G.spacing[0]), R(G.spacing[1]), R(G.spacing[2])};
+        const R t = box_entry<R>(p, d, o, e, face_tol<R>(sp));
         best = t < best ? t : best;
     }
     return best;
+}
+
+// Ray p + t d against the closed box [lo, lo + ext]: the parameter interval [t0, t1] inside
+// it (t0 > t1 when the ray misses).
+template <typename R>
+__device__ __forceinline__ void box_span(const V3<R>& p, const V3<R>& d, const V3<R>& lo, const V3<R>& ext, R& t0,
+                                         R& t1) {
+    t0 = -R(INFINITY);
+    t1 = R(INFINITY);
+    const R pp[3] = {p.x, p.y, p.z}, dd[3] = {d.x, d.y, d.z}, ll[3] = {lo.x, lo.y, lo.z}, ee[3] = {ext.x, ext.y, ext.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (dd[a] == R(0)) {
+            if (pp[a] < ll[a] || pp[a] > ll[a] + ee[a]) {
+                t0 = R(INFINITY);
+                t1 = -R(INFINITY);
+            }
+            continue;
+        }
+        R u1 = (ll[a] - pp[a]) / dd[a], u2 = (ll[a] + ee[a] - pp[a]) / dd[a];
+        if (u1 > u2) {
+            const R t = u1;
+            u1 = u2;
+            u2 = t;
+        }
+        t0 = u1 > t0 ? u1 : t0;
+        t1 = u2 < t1 ? u2 : t1;
+    }
+}
+
+constexpr int kCellWalkLimit = 4096;  // cells one flight crosses at most (then it ends on a cell face)
+
+// A flight of the opt-in tracking modes that reaches a face (a grid entered from the
+// background, a grid left, the walk limit) goes on past it for kCutSliver cm against the
+// global majorant, valid everywhere, with the optical depth it has left: it ends inside that
+// sliver at a tentative collision, or at the sliver's far end.  Flights therefore never stop
+// on a face, so a tally plane or AACuboid face lying on a grid face sees each crossing in
+// exactly one segment, whatever the rounding of the positions (about 1e-5 cm at 100 cm in
+// FP32).
+constexpr double kCutSliver = 1e-4;
+
+// Macro-cell flight (MIDSX_TRACK_MACRO_CELL) from p along d with optical depth tau.  The
+// grid the ray is in (first-hit order, p inside or on a face it enters through) is walked
+// cell by cell (Amanatides-Woo): a cell of material mask m has the majorant
+// max_{k in m} mu[k * stride] at the photon's energy, and the depth is spent there.
+// Returns 0: the depth runs out at s in a cell of majorant mu_c (tentative collision);
+// 1: the walk reaches the grid's face at s (or a cell face after kCellWalkLimit cells) with
+// the depth tau_rem left; 2: no grid holds the ray's start (background).
+template <typename R, bool MX>
+__device__ __forceinline__ int cell_flight(const Geo<R>& g, const R* mu, int stride, const V3<R>& p, const V3<R>& d,
+                                           R tau, R& s, R& mu_c, R& tau_rem) {
+    // which grid: the first whose box holds the start within the rounding allowance of its
+    // faces (t0 <= tol) and that the ray does not leave within that allowance (t1 > tol:
+    // a flight that ended on a grid's far face continues in the background)
+    V3<R> org = g.org, ext = g.ext, spc = g.spc;
+    int cn[3] = {g.cnx, g.cny, g.cnz};
+    const uint32_t* cells = g.cells;
+    R t0, t1;
+    box_span<R>(p, d, org, ext, t0, t1);
+    R tol = face_tol<R>(spc);
+    bool found = t0 <= tol && t1 > tol && t0 <= t1;
+    for (int k = 0; !found && k + 1 < g.n_grids; ++k) {
+        const DevGrid& G = g.extra[k];
+        if constexpr (MX) {
+            org = {G.f_origin[0], G.f_origin[1], G.f_origin[2]};
+            ext = {G.f_ext[0], G.f_ext[1], G.f_ext[2]};
+        } else {
+            org = {G.origin[0], G.origin[1], G.origin[2]};
+            ext = {G.ext[0], G.ext[1], G.ext[2]};
+        }
+        spc = {R(G.spacing[0]), R(G.spacing[1]), R(G.spacing[2])};
+        box_span<R>(p, d, org, ext, t0, t1);
+        tol = face_tol<R>(spc);
+        found = t0 <= tol && t1 > tol && t0 <= t1;
+        if (found) {
+            cn[0] = G.cdims[0];
+            cn[1] = G.cdims[1];
+            cn[2] = G.cdims[2];
+            cells = g.cells + G.cell_offset;
+        }
+    }
+    if (!found) return 2;
+    // start cell: from the point a little inside along the ray, clamped into the grid
+    R t = t0 > R(0) ? t0 : R(0);
+    const R edge = R(1 << g.cshift);
+    const R csz[3] = {spc.x * edge, spc.y * edge, spc.z * edge};
+    const R pp[3] = {p.x, p.y, p.z}, dd[3] = {d.x, d.y, d.z}, oo[3] = {org.x, org.y, org.z};
+    const R tend = t1 < t + tol ? t1 : t + tol;
+    const R tin = t + R(0.5) * (tend - t);  // the start cell is the one holding p + tin d
+    int c[3], step[3];
+    R tnext[3], tdelta[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const R q = (pp[a] + tin * dd[a] - oo[a]) / csz[a];
+        int ci = q >= R(0) ? int(q) : 0;
+        ci = ci >= cn[a] ? cn[a] - 1 : ci;
+        c[a] = ci;
+        if (dd[a] > R(0)) {
+            step[a] = 1;
+            tnext[a] = (oo[a] + R(ci + 1) * csz[a] - pp[a]) / dd[a];
+            tdelta[a] = csz[a] / dd[a];
+        } else if (dd[a] < R(0)) {
+            step[a] = -1;
+            tnext[a] = (oo[a] + R(ci) * csz[a] - pp[a]) / dd[a];
+            tdelta[a] = -csz[a] / dd[a];
+        } else {
+            step[a] = 0;
+            tnext[a] = R(INFINITY);
+            tdelta[a] = R(INFINITY);
+        }
+    }
+    for (int it = 0; it < kCellWalkLimit; ++it) {
+        const uint32_t m = __ldg(cells + (size_t(c[2]) * cn[1] + c[1]) * cn[0] + c[0]);
+        R mc = R(0);
+        for (uint32_t b = m; b; b &= b - 1u) {
+            const R v = mu[(__ffs(int(b)) - 1) * stride];
+            mc = v > mc ? v : mc;
+        }
+        const int a = tnext[0] < tnext[1] ? (tnext[0] < tnext[2] ? 0 : 2) : (tnext[1] < tnext[2] ? 1 : 2);
+        R tn = tnext[a] < t1 ? tnext[a] : t1;
+        tn = tn > t ? tn : t;
+        const R depth = mc * (tn - t);
+        if (tau < depth) {
+            s = t + tau / mc;
+            mu_c = mc;
+            return 0;
+        }
+        tau -= depth;
+        t = tn;
+        if (tn >= t1) break;
+        c[a] += step[a];
+        if (c[a] < 0 || c[a] >= cn[a]) break;
+        tnext[a] += tdelta[a];
+    }
+    s = t;
+    mu_c = R(0);
+    tau_rem = tau;
+    return 1;
 }
 
 // ComputationalDomain::getVoxel (computational_domain.cpp:23-31) for a point of the domain:

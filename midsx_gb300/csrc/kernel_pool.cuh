@@ -66,11 +66,11 @@ __host__ __device__ inline size_t pool_smem(int n_jobs, bool multi, int n_materi
            size_t(block / 32) * 2 * kPoolSlots;
 }
 
-// FAST = MIDSX_TRACK_BACKGROUND_FAST (a kernel of its own: compiled into one kernel with the
-// reference tracking, the fast path's code cost the reference path 8 %).  Batched launches
-// take blocks of up to 256 threads: their per-job counters and geometry in shared memory
-// (~16 KB for 64 jobs) are then shared by twice the photon slots.
-template <typename R, bool MULTI, bool FAST>
+// TRACK = midsx_tracking, each a kernel of its own (compiled into one kernel with the
+// reference tracking, the background fast path's code cost the reference path 8 %).  Batched
+// launches take blocks of up to 256 threads: their per-job counters and geometry in shared
+// memory (~16 KB for 64 jobs) are then shared by twice the photon slots.
+template <typename R, bool MULTI, int TRACK>
 __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3 : 6) : (MULTI ? 2 : 4))
     transport_pool_kernel(const RunParams P) {
     constexpr bool MX = sizeof(R) == 4;
@@ -126,7 +126,8 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
     const Geo<R> g0 = make_geo<R>(P.job0.G);
     const unsigned long long epoch = P.epoch ? *P.epoch : 0ull;
     const int regroup = max(1, min(P.regroup, 32));
-    constexpr bool fast_mode = FAST;
+    constexpr bool fast_mode = TRACK != MIDSX_TRACK_REFERENCE;   // background flights
+    constexpr bool macro_mode = TRACK == MIDSX_TRACK_MACRO_CELL;  // and macro-cell flights in grids
     int rdy_top = 0, ev_top = kPoolSlots;  // warp-uniform list sizes
     bool exhausted = false;                // warp-uniform: every history of the launch handed out
 
@@ -242,16 +243,47 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
                 // MIDSX_TRACK_BACKGROUND_FAST: a photon known to be in the background (vox == -1
                 // after its last voxel lookup) flies against the background's own attenuation,
                 // exact there, up to the first grid it would enter
-                const bool fast = fast_mode && vox == -1;
-                R lim = R(INFINITY);  // distance to the first grid on the way (fast flights)
-                if (fast) {
-                    const R mu_bg = S.mu[g.bg * ns + cur];
+                // MIDSX_TRACK_MACRO_CELL: any other photon spends one optical depth through the
+                // macro cells of the grid it is in.  fl: -1 a reference step; 0 a tentative
+                // collision against the cell majorant mu_c; 1 a flight that ends, without
+                // interaction, kCutSliver past a face; 2 a tentative collision in that sliver
+                // (against the global majorant); 3 a background collision (always real)
+                int fl = -1;
+                R mu_c = R(0);
+                if (fast_mode) {
+                    R tau, tau_rem = R(0), lim = R(INFINITY);
                     if constexpr (MX)
-                        s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) / mu_bg;
+                        tau = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f);
                     else
-                        s = -log_(to_uniform(w1, R(0))) / mu_bg;
-                    lim = grid_entry<R, MX>(g, pos, dir);
-                    if (lim <= s) s = lim;
+                        tau = -log_(to_uniform(w1, R(0)));
+                    bool bg = vox == -1;
+                    if (macro_mode && !bg) {
+                        fl = cell_flight<R, MX>(g, S.mu + cur, ns, pos, dir, tau, s, mu_c, tau_rem);
+                        bg = fl == 2;
+                    }
+                    if (bg) {
+                        const R mu_bg = S.mu[g.bg * ns + cur];
+                        s = tau / mu_bg;
+                        lim = grid_entry<R, MX>(g, pos, dir);
+                        fl = 3;
+                        if (s > lim) {
+                            tau_rem = tau - mu_bg * lim;
+                            s = lim;
+                            fl = 1;
+                        }
+                    }
+                    if (fl == 1) {
+                        const R past = tau_rem * inv_mu_max;
+                        if (past < R(kCutSliver)) {
+                            s += past;
+                            fl = 2;
+                        } else {
+                            s += R(kCutSliver);
+                        }
+                    }
+                }
+                if (fl >= 0) {
+                    // s from the flight above
                 } else if constexpr (MX) {
                     s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) * inv_mu_max;
                 } else {
@@ -264,17 +296,24 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
                     stat_add(st, kStEscE, fx_stat(E));
                     segment = true;
                     park = kKindStart;
-                } else if (fast) {
+                } else if (fl == 3) {
                     mat = g.bg;
-                    if (s == lim) {
-                        // on a grid face, no interaction: the next flight is a reference step
-                        // (global majorant, valid everywhere) from here
-                        vox = -2;
+                    vox = -1;
+                    park = kKindCollide;  // every background collision is real
+                } else if (fl == 1) {
+                    // past a face, no interaction: the next flight finds its region from here
+                    // (BACKGROUND_FAST: a reference step, valid everywhere)
+                    vox = -2;
+                    segment = true;
+                } else if (fl == 0) {
+                    // real with probability mu(voxel) / mu(cell); a voxel met across a cell face
+                    // by rounding, with a larger attenuation than the cell's, interacts
+                    locate<R, MX>(g, pos, vox, mat, fetches, st);
+                    const R mm = S.mu[mat * ns + cur];
+                    if (to_uniform(w2, R(0)) * mu_c < mu_c - mm)
                         segment = true;
-                    } else {
-                        vox = -1;
-                        park = kKindCollide;  // every background collision is real
-                    }
+                    else
+                        park = kKindCollide;
                 } else {
                     locate<R, MX>(g, pos, vox, mat, fetches, st);
                     if (to_uniform(w2, R(0)) < S.thr[mat * ns + cur])

@@ -68,8 +68,15 @@ struct DevGrid {
     double origin[3], spacing[3], ext[3];
     float f_origin[3], f_ext[3], f_ispc[3];
     int dims[3];
-    int offset;  // number of the grid's first voxel in the phantom (ids and dose tally)
+    int offset;       // number of the grid's first voxel in the phantom (ids and dose tally)
+    int cdims[3];     // macro cells along each axis
+    int cell_offset;  // number of the grid's first macro cell in the phantom
 };
+
+// Macro cells: 2^cell_shift voxels along each edge (fewer at the grid's far faces), a bit
+// mask of the dense material indices present, cells x fastest, grid after grid.
+constexpr int kCellShiftDefault = 3;
+static_assert((1 << kCellShiftDefault) == MIDSX_MACRO_CELL, "MIDSX_MACRO_CELL is the default edge");
 
 struct DevGeom {
     double domain[3], origin[3], spacing[3], ext[3];
@@ -78,6 +85,9 @@ struct DevGeom {
     const uint8_t* ids;     // every grid's dense material indices, grid after grid
     int n_grids;            // grids of the domain (1 = the first alone)
     const DevGrid* extra;   // n_grids - 1 further grids (device memory), in first-hit order
+    const uint32_t* cells;  // macro-cell material masks of every grid
+    int cdims[3];           // macro cells of the first grid along each axis
+    int cell_shift;         // macro-cell edge = 2^cell_shift voxels
 };
 
 // One simulation: geometry, source, tallies and its history range [first, first + n) of its
@@ -439,6 +449,36 @@ __global__ void remap_kernel(const uint8_t* in, uint8_t* out, const uint8_t* lut
     }
 }
 
+// Material mask of each macro cell of one grid: OR of 1 << material over the cell's voxels.
+__global__ void cell_mask_kernel(const uint8_t* ids, int nx, int ny, int nz, int cnx, int cny, int cnz, int shift,
+                                 uint32_t* cells) {
+    const size_t n = size_t(cnx) * cny * cnz;
+    const int edge = 1 << shift;
+    for (size_t c = size_t(blockIdx.x) * blockDim.x + threadIdx.x; c < n; c += size_t(gridDim.x) * blockDim.x) {
+        const int cx = int(c % cnx), cy = int((c / cnx) % cny), cz = int(c / (size_t(cnx) * cny));
+        const int x0 = cx << shift, y0 = cy << shift, z0 = cz << shift;
+        const int x1 = min(x0 + edge, nx), y1 = min(y0 + edge, ny), z1 = min(z0 + edge, nz);
+        uint32_t m = 0;
+        for (int z = z0; z < z1; ++z)
+            for (int y = y0; y < y1; ++y) {
+                const uint8_t* row = ids + (size_t(z) * ny + y) * nx;
+                for (int x = x0; x < x1; ++x) m |= 1u << (row[x] & 31);
+            }
+        cells[c] = m;
+    }
+}
+
+// ORs `bits` into the cells [lo, hi] (inclusive) of one grid's cell array.
+__global__ void cell_or_box_kernel(uint32_t* cells, int cnx, int cny, int lx, int ly, int lz, int hx, int hy, int hz,
+                                   uint32_t bits) {
+    const int wx = hx - lx + 1, wy = hy - ly + 1, wz = hz - lz + 1;
+    const size_t n = size_t(wx) * wy * wz;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const int x = lx + int(i % wx), y = ly + int((i / wx) % wy), z = lz + int(i / (size_t(wx) * wy));
+        cells[(size_t(z) * cny + y) * cnx + x] |= bits;
+    }
+}
+
 __global__ void f64_to_f32_kernel(const double* in, float* out, size_t n) {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n) out[i] = float(in[i]);
@@ -465,6 +505,9 @@ struct midsx_gpu_phantom {
     uint8_t* ids = nullptr;
     size_t n_voxels = 0;                       // all grids
     DevGrid* extra = nullptr;                  // grids after the first (device)
+    uint32_t* cells = nullptr;                 // macro-cell material masks (device)
+    std::vector<midsx_grid_spec> grids;        // every grid's geometry (ids pointers cleared)
+    std::vector<DevGrid> host_extra;           // host copy of `extra`
     const midsx_gpu_tables* tables = nullptr;  // the tables its dense material indices refer to
 };
 
@@ -703,6 +746,76 @@ namespace {
 
 // Uploads the grids' voxel ids (concatenated, grid after grid), remaps them to the tables'
 // dense material indices and fills the domain description.
+// Macro-cell masks of every grid with edges of 2^shift voxels (synchronous); the cells of a
+// grid that meet an earlier grid's box (the earlier grid owns the overlap) take every
+// material of the tables.  Replaces the phantom's previous cells.
+midsx_status build_cells(midsx_gpu_phantom* p, int shift) {
+    if (!p->ids) {
+        set_last_error("the phantom's voxels are not resident");
+        return MIDSX_INVALID_ARG;
+    }
+    const int n_grids = int(p->grids.size());
+    auto cdim = [shift](int n) { return (n + (1 << shift) - 1) >> shift; };
+    std::vector<size_t> cell_off(size_t(n_grids) + 1, 0);
+    for (int k = 0; k < n_grids; ++k) {
+        size_t c = 1;
+        for (int i = 0; i < 3; ++i) c *= size_t(cdim(p->grids[size_t(k)].dims[i]));
+        cell_off[size_t(k) + 1] = cell_off[size_t(k)] + c;
+    }
+    uint32_t* cells = nullptr;
+    if (!cuda_ok(cudaMalloc(&cells, cell_off.back() * sizeof(uint32_t)), "cudaMalloc")) return MIDSX_OOM;
+    const uint32_t all_bits =
+        p->tables->T.n_materials >= 32 ? ~0u : ((1u << p->tables->T.n_materials) - 1u);
+    const int sms = p->tables->sm_count;
+    bool good = true;
+    size_t voff = 0;
+    for (int k = 0; good && k < n_grids; ++k) {
+        const midsx_grid_spec& g = p->grids[size_t(k)];
+        const int cnx = cdim(g.dims[0]), cny = cdim(g.dims[1]), cnz = cdim(g.dims[2]);
+        uint32_t* gc = cells + cell_off[size_t(k)];
+        cell_mask_kernel<<<sms * 4, 256>>>(p->ids + voff, g.dims[0], g.dims[1], g.dims[2], cnx, cny, cnz, shift, gc);
+        good = cuda_ok(cudaGetLastError(), "cell_mask_kernel");
+        for (int j = 0; good && j < k; ++j) {
+            const midsx_grid_spec& e = p->grids[size_t(j)];
+            int lo[3], hi[3];
+            bool meets = true;
+            for (int i = 0; i < 3; ++i) {
+                const double csz = g.spacing[i] * double(1 << shift);
+                const double a = e.origin[i] - g.origin[i], b = a + e.dims[i] * e.spacing[i];
+                const double ext = g.dims[i] * g.spacing[i];
+                if (b < 0 || a > ext) meets = false;
+                const int cmax = cdim(g.dims[i]);
+                lo[i] = std::max(0, std::min(cmax - 1, int(std::floor(a / csz)) - 1));
+                hi[i] = std::max(0, std::min(cmax - 1, int(std::floor(b / csz)) + 1));
+            }
+            if (!meets) continue;
+            cell_or_box_kernel<<<sms, 256>>>(gc, cnx, cny, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], all_bits);
+            good = cuda_ok(cudaGetLastError(), "cell_or_box_kernel");
+        }
+        voff += size_t(g.dims[0]) * g.dims[1] * g.dims[2];
+    }
+    for (int k = 1; k < n_grids; ++k) {
+        DevGrid& d = p->host_extra[size_t(k) - 1];
+        for (int i = 0; i < 3; ++i) d.cdims[i] = cdim(d.dims[i]);
+        d.cell_offset = int(cell_off[size_t(k)]);
+    }
+    if (good && n_grids > 1)
+        good = cuda_ok(cudaMemcpy(p->extra, p->host_extra.data(), sizeof(DevGrid) * p->host_extra.size(),
+                                  cudaMemcpyHostToDevice),
+                       "cudaMemcpy");
+    if (good) good = cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    if (!good) {
+        cudaFree(cells);
+        return MIDSX_CUDA_ERROR;
+    }
+    cudaFree(p->cells);
+    p->cells = cells;
+    p->G.cells = cells;
+    p->G.cell_shift = shift;
+    for (int i = 0; i < 3; ++i) p->G.cdims[i] = cdim(p->grids[0].dims[i]);
+    return MIDSX_OK;
+}
+
 midsx_status phantom_create_impl(midsx_tables_h tables, const double* domain, int32_t background_id,
                                  const midsx_grid_spec* grids, int n_grids, midsx_phantom_h* out) {
     if (!tables || !domain || !grids || !out || n_grids < 1 || n_grids > MIDSX_MAX_GRIDS) {
@@ -783,10 +896,7 @@ midsx_status phantom_create_impl(midsx_tables_h tables, const double* domain, in
         off += n;
     }
     bool good = cuda_ok(cudaMemcpy(dlut, lut, 256, cudaMemcpyHostToDevice), "cudaMemcpy") &&
-                cuda_ok(cudaMemset(bad, 0, sizeof(int)), "cudaMemset") &&
-                (extra.empty() || cuda_ok(cudaMemcpy(p->extra, extra.data(), sizeof(DevGrid) * extra.size(),
-                                                     cudaMemcpyHostToDevice),
-                                          "cudaMemcpy"));
+                cuda_ok(cudaMemset(bad, 0, sizeof(int)), "cudaMemset");
     int hbad = 0;
     if (good) {
         remap_kernel<<<tables->sm_count * 8, 256>>>(raw, p->ids, dlut, total, bad);
@@ -817,6 +927,14 @@ midsx_status phantom_create_impl(midsx_tables_h tables, const double* domain, in
     G.n_grids = n_grids;
     G.extra = p->extra;
     p->tables = tables;
+    p->grids.assign(grids, grids + n_grids);
+    for (auto& gs : p->grids) gs.ids = nullptr;
+    p->host_extra = extra;
+    const midsx_status cst = build_cells(p, kCellShiftDefault);
+    if (cst != MIDSX_OK) {
+        midsx_gpu_phantom_destroy(p);
+        return cst;
+    }
     *out = p;
     return MIDSX_OK;
 }
@@ -843,10 +961,21 @@ extern "C" midsx_status midsx_gpu_phantom_create_grids(midsx_tables_h tables, co
     return phantom_create_impl(tables, domain, background_id, grids, n_grids, out);
 }
 
+extern "C" midsx_status midsx_gpu_phantom_macro_cells(midsx_phantom_h p, int32_t edge) {
+    if (!p || edge < 1 || edge > 64 || (edge & (edge - 1))) {
+        set_last_error("midsx_gpu_phantom_macro_cells: edge is a power of two in [1, 64]");
+        return MIDSX_INVALID_ARG;
+    }
+    int shift = 0;
+    while ((1 << shift) < edge) ++shift;
+    return build_cells(p, shift);
+}
+
 extern "C" midsx_status midsx_gpu_phantom_destroy(midsx_phantom_h p) {
     if (!p) return MIDSX_INVALID_ARG;
     cudaFree(p->ids);
     cudaFree(p->extra);
+    cudaFree(p->cells);
     delete p;
     return MIDSX_OK;
 }
@@ -1180,16 +1309,16 @@ midsx_status launch_typed(midsx_tables_h tables, const RunParams& P, const midsx
     return MIDSX_OK;
 }
 
-template <typename R, bool MULTI, bool FAST>
+template <typename R, bool MULTI, int TRACK>
 midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_run_config& cfg, int block,
                          cudaStream_t s) {
     const size_t smem = pool_smem<R>(P.n_jobs, MULTI, tables->T.n_materials, block);
     if (smem > 48 * 1024)
-        CUDA_TRY(cudaFuncSetAttribute(transport_pool_kernel<R, MULTI, FAST>,
+        CUDA_TRY(cudaFuncSetAttribute(transport_pool_kernel<R, MULTI, TRACK>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = cfg.blocks_per_sm;
     if (per_sm <= 0) {
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_pool_kernel<R, MULTI, FAST>, block,
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_pool_kernel<R, MULTI, TRACK>, block,
                                                                smem));
         per_sm = std::max(per_sm, 1);
     }
@@ -1200,7 +1329,7 @@ midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_
     // a warp keeps two photons per lane in flight
     uint64_t want = (P.total + 2 * uint64_t(block) - 1) / (2 * uint64_t(block));
     uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(tables->sm_count) * per_sm));
-    transport_pool_kernel<R, MULTI, FAST><<<unsigned(grid), block, smem, s>>>(P);
+    transport_pool_kernel<R, MULTI, TRACK><<<unsigned(grid), block, smem, s>>>(P);
     CUDA_TRY(cudaGetLastError());
     return MIDSX_OK;
 }
@@ -1208,8 +1337,14 @@ midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_
 template <typename R, bool MULTI>
 midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_run_config& cfg, int block,
                          cudaStream_t s) {
-    return P.tracking == MIDSX_TRACK_BACKGROUND_FAST ? launch_pool<R, MULTI, true>(tables, P, cfg, block, s)
-                                                     : launch_pool<R, MULTI, false>(tables, P, cfg, block, s);
+    switch (P.tracking) {
+        case MIDSX_TRACK_BACKGROUND_FAST:
+            return launch_pool<R, MULTI, MIDSX_TRACK_BACKGROUND_FAST>(tables, P, cfg, block, s);
+        case MIDSX_TRACK_MACRO_CELL:
+            return launch_pool<R, MULTI, MIDSX_TRACK_MACRO_CELL>(tables, P, cfg, block, s);
+        default:
+            return launch_pool<R, MULTI, MIDSX_TRACK_REFERENCE>(tables, P, cfg, block, s);
+    }
 }
 
 // Completes the launch parameters from cfg, zeroes the history counter and launches.  The
@@ -1220,14 +1355,14 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
         set_last_error("unknown scheduler");
         return MIDSX_INVALID_ARG;
     }
-    if (cfg.tracking != MIDSX_TRACK_REFERENCE && cfg.tracking != MIDSX_TRACK_BACKGROUND_FAST) {
+    if (cfg.tracking < MIDSX_TRACK_REFERENCE || cfg.tracking > MIDSX_TRACK_MACRO_CELL) {
         set_last_error("unknown tracking");
         return MIDSX_INVALID_ARG;
     }
     const bool pool = cfg.scheduler != MIDSX_SCHED_LANES && P.trace == nullptr &&
                       (cfg.scheduler == MIDSX_SCHED_POOL || kDefaultScheduler == MIDSX_SCHED_POOL);
-    if (cfg.tracking == MIDSX_TRACK_BACKGROUND_FAST && !pool) {
-        set_last_error("background fast tracking runs in the photon-pool scheduler only");
+    if (cfg.tracking != MIDSX_TRACK_REFERENCE && !pool) {
+        set_last_error("background fast and macro-cell tracking run in the photon-pool scheduler only");
         return MIDSX_INVALID_ARG;
     }
     P.tracking = cfg.tracking;

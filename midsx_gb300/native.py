@@ -17,7 +17,8 @@ MAX_ENERGY_BINS = 65536
 OK, INVALID_ARG, OOM, TIMEOUT, STEP_CAP, TABLE_RANGE, CUDA_ERROR, NOT_FOUND, IO_ERROR = range(9)
 PREC_FP64, PREC_MIXED = 0, 1
 SCHED_DEFAULT, SCHED_LANES, SCHED_POOL = 0, 1, 2
-TRACK_REFERENCE, TRACK_BACKGROUND_FAST = 0, 1
+TRACK_REFERENCE, TRACK_BACKGROUND_FAST, TRACK_MACRO_CELL = 0, 1, 2
+MACRO_CELL = 8  # voxels per macro-cell edge (MIDSX_MACRO_CELL)
 DIR_BEAM, DIR_ISOTROPIC, DIR_RECTANGLE, DIR_DISC = range(4)
 SPEC_MONO, SPEC_POLY = 0, 1
 TALLY_DISC, TALLY_RECT, TALLY_BINNED_RECT, TALLY_AACUBOID = 1, 2, 3, 4
@@ -158,6 +159,7 @@ _SIGNATURES = {
     "midsx_gpu_tables_destroy": (C.c_int, [VP]),
     "midsx_gpu_phantom_create": (C.c_int, [VP, C.POINTER(GeometrySpec), C.c_void_p, C.POINTER(VP)]),
     "midsx_gpu_phantom_destroy": (C.c_int, [VP]),
+    "midsx_gpu_phantom_macro_cells": (C.c_int, [VP, C.c_int32]),
     "midsx_gpu_phantom_create_grids": (C.c_int, [VP, C.POINTER(C.c_double), C.c_int32, C.POINTER(GridSpec), C.c_int32,
                                                  C.POINTER(VP)]),
     "midsx_gpu_source_create": (C.c_int, [C.POINTER(SourceSpec), C.POINTER(VP)]),
