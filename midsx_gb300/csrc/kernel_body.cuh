@@ -290,37 +290,58 @@ __device__ __forceinline__ int cell_flight(const Geo<R>& g, const R* mu, int str
     const R pp[3] = {p.x, p.y, p.z}, dd[3] = {d.x, d.y, d.z}, oo[3] = {org.x, org.y, org.z};
     const R tend = t1 < t + tol ? t1 : t + tol;
     const R tin = t + R(0.5) * (tend - t);  // the start cell is the one holding p + tin d
-    int c[3], step[3];
-    R tnext[3], tdelta[3];
+    // per axis: the next cell face along the ray (tn*), the distance between faces (dt*), the
+    // cell index step (inc*) and the cells left before the grid's side (left*) - scalars, so
+    // that the walk stays in registers
+    R tn3[3], dt3[3];
+    int inc3[3], left3[3], idx = 0, stride3 = 1;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const R q = (pp[a] + tin * dd[a] - oo[a]) / csz[a];
         int ci = q >= R(0) ? int(q) : 0;
         ci = ci >= cn[a] ? cn[a] - 1 : ci;
-        c[a] = ci;
+        idx += ci * stride3;
         if (dd[a] > R(0)) {
-            step[a] = 1;
-            tnext[a] = (oo[a] + R(ci + 1) * csz[a] - pp[a]) / dd[a];
-            tdelta[a] = csz[a] / dd[a];
+            inc3[a] = stride3;
+            left3[a] = cn[a] - 1 - ci;
+            tn3[a] = (oo[a] + R(ci + 1) * csz[a] - pp[a]) / dd[a];
+            dt3[a] = csz[a] / dd[a];
         } else if (dd[a] < R(0)) {
-            step[a] = -1;
-            tnext[a] = (oo[a] + R(ci) * csz[a] - pp[a]) / dd[a];
-            tdelta[a] = -csz[a] / dd[a];
+            inc3[a] = -stride3;
+            left3[a] = ci;
+            tn3[a] = (oo[a] + R(ci) * csz[a] - pp[a]) / dd[a];
+            dt3[a] = -csz[a] / dd[a];
         } else {
-            step[a] = 0;
-            tnext[a] = R(INFINITY);
-            tdelta[a] = R(INFINITY);
+            inc3[a] = 0;
+            left3[a] = 0;
+            tn3[a] = R(INFINITY);
+            dt3[a] = R(INFINITY);
         }
+        stride3 *= cn[a];
     }
+    R tnx = tn3[0], tny = tn3[1], tnz = tn3[2];
+    const R dtx = dt3[0], dty = dt3[1], dtz = dt3[2];
+    const int incx = inc3[0], incy = inc3[1], incz = inc3[2];
+    int leftx = left3[0], lefty = left3[1], leftz = left3[2];
+    // the next cell's mask is loaded while this cell is evaluated, and a cell with the mask of
+    // the one before reuses its majorant
+    uint32_t m = __ldg(cells + idx), m_prev = 0u;
+    R mc = R(0);
     for (int it = 0; it < kCellWalkLimit; ++it) {
-        const uint32_t m = __ldg(cells + (size_t(c[2]) * cn[1] + c[1]) * cn[0] + c[0]);
-        R mc = R(0);
-        for (uint32_t b = m; b; b &= b - 1u) {
-            const R v = mu[(__ffs(int(b)) - 1) * stride];
-            mc = v > mc ? v : mc;
+        const int a = tnx < tny ? (tnx < tnz ? 0 : 2) : (tny < tnz ? 1 : 2);
+        const R tf = a == 0 ? tnx : (a == 1 ? tny : tnz);
+        const int left = a == 0 ? leftx : (a == 1 ? lefty : leftz);
+        const int nidx = idx + (a == 0 ? incx : (a == 1 ? incy : incz));
+        const uint32_t mn = left > 0 ? __ldg(cells + nidx) : 0u;
+        if (m != m_prev) {
+            mc = R(0);
+            for (uint32_t b = m; b; b &= b - 1u) {
+                const R v = mu[(__ffs(int(b)) - 1) * stride];
+                mc = v > mc ? v : mc;
+            }
+            m_prev = m;
         }
-        const int a = tnext[0] < tnext[1] ? (tnext[0] < tnext[2] ? 0 : 2) : (tnext[1] < tnext[2] ? 1 : 2);
-        R tn = tnext[a] < t1 ? tnext[a] : t1;
+        R tn = tf < t1 ? tf : t1;
         tn = tn > t ? tn : t;
         const R depth = mc * (tn - t);
         if (tau < depth) {
@@ -330,10 +351,19 @@ __device__ __forceinline__ int cell_flight(const Geo<R>& g, const R* mu, int str
         }
         tau -= depth;
         t = tn;
-        if (tn >= t1) break;
-        c[a] += step[a];
-        if (c[a] < 0 || c[a] >= cn[a]) break;
-        tnext[a] += tdelta[a];
+        if (tn >= t1 || left <= 0) break;
+        idx = nidx;
+        m = mn;
+        if (a == 0) {
+            --leftx;
+            tnx += dtx;
+        } else if (a == 1) {
+            --lefty;
+            tny += dty;
+        } else {
+            --leftz;
+            tnz += dtz;
+        }
     }
     s = t;
     mu_c = R(0);
