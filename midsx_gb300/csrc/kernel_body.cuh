@@ -120,9 +120,6 @@ struct Geo {
     const uint8_t* ids;
     int n_grids;           // grids of the domain; the first is held above
     const DevGrid* extra;  // the others, in first-hit order
-    const uint32_t* cells; // macro-cell material masks (every grid)
-    int cnx, cny, cnz;     // macro cells of the first grid
-    int cshift;            // macro-cell edge = 2^cshift voxels
 };
 
 template <typename R>
@@ -140,11 +137,6 @@ __device__ Geo<R> make_geo(const DevGeom& G) {
     g.ids = G.ids;
     g.n_grids = G.n_grids;
     g.extra = G.extra;
-    g.cells = G.cells;
-    g.cnx = G.cdims[0];
-    g.cny = G.cdims[1];
-    g.cnz = G.cdims[2];
-    g.cshift = G.cell_shift;
     return g;
 }
 
@@ -242,7 +234,8 @@ constexpr int kCellWalkLimit = 4096;  // cells one flight crosses at most (then 
 // FP32).
 constexpr double kCutSliver = 1e-4;
 
-// Macro-cell flight (MIDSX_TRACK_MACRO_CELL) from p along d with optical depth tau.  The
+// Macro-cell flight (MIDSX_TRACK_MACRO_CELL) from p along d with optical depth tau; the
+// cells come from the job's DevGeom (kept out of Geo, which the reference path holds).  The
 // grid the ray is in (first-hit order, p inside or on a face it enters through) is walked
 // cell by cell (Amanatides-Woo): a cell of material mask m has the majorant
 // max_{k in m} mu[k * stride] at the photon's energy, and the depth is spent there.
@@ -250,14 +243,14 @@ constexpr double kCutSliver = 1e-4;
 // 1: the walk reaches the grid's face at s (or a cell face after kCellWalkLimit cells) with
 // the depth tau_rem left; 2: no grid holds the ray's start (background).
 template <typename R, bool MX>
-__device__ __forceinline__ int cell_flight(const Geo<R>& g, const R* mu, int stride, const V3<R>& p, const V3<R>& d,
-                                           R tau, R& s, R& mu_c, R& tau_rem) {
+__device__ __forceinline__ int cell_flight(const Geo<R>& g, const DevGeom& D, const R* mu, int stride, const V3<R>& p,
+                                           const V3<R>& d, R tau, R& s, R& mu_c, R& tau_rem) {
     // which grid: the first whose box holds the start within the rounding allowance of its
     // faces (t0 <= tol) and that the ray does not leave within that allowance (t1 > tol:
     // a flight that ended on a grid's far face continues in the background)
     V3<R> org = g.org, ext = g.ext, spc = g.spc;
-    int cn[3] = {g.cnx, g.cny, g.cnz};
-    const uint32_t* cells = g.cells;
+    int cn[3] = {D.cdims[0], D.cdims[1], D.cdims[2]};
+    const uint32_t* cells = D.cells;
     R t0, t1;
     box_span<R>(p, d, org, ext, t0, t1);
     R tol = face_tol<R>(spc);
@@ -279,13 +272,13 @@ __device__ __forceinline__ int cell_flight(const Geo<R>& g, const R* mu, int str
             cn[0] = G.cdims[0];
             cn[1] = G.cdims[1];
             cn[2] = G.cdims[2];
-            cells = g.cells + G.cell_offset;
+            cells = D.cells + G.cell_offset;
         }
     }
     if (!found) return 2;
     // start cell: from the point a little inside along the ray, clamped into the grid
     R t = t0 > R(0) ? t0 : R(0);
-    const R edge = R(1 << g.cshift);
+    const R edge = R(1 << D.cell_shift);
     const R csz[3] = {spc.x * edge, spc.y * edge, spc.z * edge};
     const R pp[3] = {p.x, p.y, p.z}, dd[3] = {d.x, d.y, d.z}, oo[3] = {org.x, org.y, org.z};
     const R tend = t1 < t + tol ? t1 : t + tol;

@@ -258,7 +258,8 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
                         tau = -log_(to_uniform(w1, R(0)));
                     bool bg = vox == -1;
                     if (macro_mode && !bg) {
-                        fl = cell_flight<R, MX>(g, S.mu + cur, ns, pos, dir, tau, s, mu_c, tau_rem);
+                        fl = cell_flight<R, MX>(g, MULTI ? P.jobs[job].G : P.job0.G, S.mu + cur, ns, pos, dir, tau,
+                                                s, mu_c, tau_rem);
                         bg = fl == 2;
                     }
                     if (bg) {
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         // collisions below) measured 3 % slower on the cone-beam dose workload and 29 % slower
         // on the radiography workload.
         if (segment && ntal > 0)
-            score_tallies<R, MX>(MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, dir, s, E,
+            score_tallies<R, MX, false>(MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, dir, s, E,
                                  scatter_class(n_coh, n_incoh), 0, false, R(0), words);
         if (cur >= 0 && park == kKindStart) end_history();
         // photons that need an event go to the event list

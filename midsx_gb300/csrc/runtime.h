@@ -27,9 +27,13 @@ midsx_status pack_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_sour
 
 // One batched launch over n_jobs records at `dev_jobs` with history offsets `dev_prefix`
 // (n_jobs + 1 words, last = total) and a history counter `dev_counter` zeroed here, on `s`.
+// spectra: some job's tallies keep an incident-energy spectrum (tallies_spectra), which the
+// lane-parking kernel scores.
 midsx_status launch_packed(midsx_tables_h tables, const void* dev_jobs, int n_jobs,
                            const unsigned long long* dev_prefix, unsigned long long total,
-                           unsigned long long* dev_counter, const midsx_run_config& cfg, cudaStream_t s);
+                           unsigned long long* dev_counter, const midsx_run_config& cfg, cudaStream_t s,
+                           bool spectra = false);
+bool tallies_spectra(midsx_tallies_h t);
 
 // Device bytes the tallies of (specs, dose_mode) take for a phantom of n_voxels voxels.
 size_t tallies_footprint(size_t n_voxels, const midsx_tally_spec* specs, int n_specs, int dose_mode);

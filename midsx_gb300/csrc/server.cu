@@ -372,8 +372,10 @@ bool midsx_gpu_server::launch_locked(bool setup_pending) {
                        "cudaMemcpyAsync");
         if (good && setup_pending) good = ok(cudaStreamWaitEvent(s.stream, setup_done, 0), "cudaStreamWaitEvent");
         if (good) good = ok(cudaEventRecord(s.start, s.stream), "cudaEventRecord");
+        bool spectra = false;
+        for (auto& p : s.parts) spectra |= midsx::rt::tallies_spectra(p.req->tallies);
         midsx_status ls = good ? midsx::rt::launch_packed(tables, s.dev_jobs, nj, s.dev_prefix, total, s.dev_counter, c,
-                                                          s.stream)
+                                                          s.stream, spectra)
                                : MIDSX_CUDA_ERROR;
         if (ls == MIDSX_OK) good = ok(cudaEventRecord(s.end, s.stream), "cudaEventRecord");
         if (ls != MIDSX_OK || !good) {

@@ -17,13 +17,11 @@
 //   kRecCubDep   AACuboid deposit: energy record at acc + 3c
 //   kRecCubEnter AACuboid entry: energy record at acc + 12 + 3c, entry count at acc + 24 + c
 //   kRecCubHit   AACuboid interaction count at acc + 28 + c
-//   kRecSpectrum spectrum bin of a scalar surface: [crossings, entrance-cosine sum] at the
-//                bin's class pair
 //   kRecDose     voxel dose: sum at rec[0]; with the full record also sum of squares rec[1]
 //                and count rec[2] (c = record stride)
 
 constexpr int kRecNone = 0, kRecSurface = 1, kRecBinned = 2, kRecCubDep = 3, kRecCubEnter = 4, kRecCubHit = 5,
-              kRecDose = 6, kRecSpectrum = 7;
+              kRecDose = 6;
 constexpr int kRecWords = 7;  // most words of one record
 
 // One word of a record: its address and the value bits to add (0 = nothing), and whether the
@@ -102,16 +100,6 @@ __device__ __forceinline__ void rec_word(int kind, unsigned long long* acc, int 
             break;
         case kRecCubDep:
             if (j < 3) vec(acc + 3 * c, j, v1, false);
-            break;
-        case kRecSpectrum:
-            if (j == 0) {
-                addr = acc;
-                bits = 1;
-            } else if (j == 1) {
-                addr = acc + 1;
-                bits = W::cosine(v1);
-                dbl = W::kDouble;
-            }
             break;
         case kRecCubEnter:
             if (j < 3) vec(acc + 12 + 3 * c, j, v1, false);
@@ -221,13 +209,11 @@ __device__ __forceinline__ void score_tallies_warp(bool active, const DevTally* 
     for (int ti = 0; ti < nt; ++ti) {
         int k1 = kRecNone, k2 = kRecNone, k3 = kRecNone;
         unsigned long long* acc = nullptr;
-        unsigned long long* acc2 = nullptr;  // record base of k2
         int c = 0;
         R v1 = R(0), v2 = R(0), e_dep = R(0);
         if (active && ti < n_tallies) {
             const DevTally& T = tallies[ti];
             acc = T.acc;
-            acc2 = T.acc;
             if (T.kind == MIDSX_TALLY_VOLUME_AACUBOID) {
                 // AACuboidVolumeTally::determineVolumeTraversal (volume_tally.cpp:38-91)
                 R lo[3], hi[3];
@@ -318,12 +304,8 @@ __device__ __forceinline__ void score_tallies_warp(bool active, const DevTally* 
                     if (E != R(0)) ++words;
                     if (ec != R(0)) ++words;
                     ++words;
-                    const int kb = T.n_energy > 0 ? energy_bin<R>(T, E) : -1;
-                    if (kb >= 0) {
-                        k2 = kRecSpectrum;
-                        acc2 = T.acc + MIDSX_SCALAR_SLOTS + (size_t(kb) * 4 + cls0) * 2;
-                        ++words;
-                    }
+                    // (no incident-energy spectra here: launches with spectrum tallies run
+                    // the lane-parking kernel)
                 }
             }
         }
@@ -331,8 +313,7 @@ __device__ __forceinline__ void score_tallies_warp(bool active, const DevTally* 
         // warp skips the records unless a lane has one (k2 and k3 only come with k1)
         if (!__any_sync(0xffffffffu, k1 != kRecNone)) continue;
         warp_record<R, MX>(k1, acc, c, v1, v2, scratch);
-        // k2: the cuboid's entry record (value E) or the surface's spectrum bin (value ec)
-        if (__any_sync(0xffffffffu, k2 != kRecNone)) warp_record<R, MX>(k2, acc2, c, v2, R(0), scratch);
+        if (__any_sync(0xffffffffu, k2 != kRecNone)) warp_record<R, MX>(k2, acc, c, v2, R(0), scratch);
         if (__any_sync(0xffffffffu, k3 != kRecNone)) warp_record<R, MX>(k3, acc, c, R(0), R(0), scratch);
     }
 }

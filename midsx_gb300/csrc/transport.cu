@@ -122,6 +122,7 @@ struct RunParams {
     int regroup;    // lanes of a warp that wait for an event before the warp runs the events
     int chunk;      // histories a lane reserves per fetch
     double* trace;  // optional (single job): energy deposited in grid voxels per history
+    int spectra;    // some tally of the launch keeps an incident-energy spectrum (lane-parking kernel)
 };
 
 // -------------------------------------------------------------------- atomics ---
@@ -185,11 +186,14 @@ __device__ __forceinline__ void vec_cosine(unsigned long long* acc, int q, int c
     ++words;
 }
 
-// One step segment [p0, p0 + s d) against every scalar/binned tally.
+// One step segment [p0, p0 + s d) against every scalar/binned tally.  SPEC: also the
+// incident-energy spectra - compiled into the lane-parking kernel only, which runs every
+// launch with a spectrum tally: in the photon-pool kernel the spectrum code, inline or out of
+// line, cost the cone-beam dose workload (no tally at all) 5 %.
 // cls0: class of the photon at the step start (surface quantities use initial_photon);
 // cls1: class of final_photon (post-interaction counts if the step interacted, else
 // a default Photon = primary), used by volume quantities.
-template <typename R, bool MX>
+template <typename R, bool MX, bool SPEC = true>
 __device__ __forceinline__ void score_tallies(const DevTally* tallies, int n_tallies, const V3<R>& p0, const V3<R>& d,
                                            R s, R E, int cls0, int cls1, bool interact, R dep, uint32_t& words) {
     for (int ti = 0; ti < n_tallies; ++ti) {
@@ -276,14 +280,16 @@ __device__ __forceinline__ void score_tallies(const DevTally* tallies, int n_tal
         vec_cosine<R, MX>(acc, 1, cls0, ec, words);
         count1(acc + 24 + cls0);
         ++words;
-        if (T.n_energy > 0) {
-            // incident-energy spectrum: [crossings, entrance-cosine sum] per bin and class
-            const int kb = energy_bin<R>(T, E);
-            if (kb >= 0) {
-                unsigned long long* sp = acc + MIDSX_SCALAR_SLOTS + (size_t(kb) * 4 + cls0) * 2;
-                count1(sp);
-                Acc<MX>::cosine(sp + 1, ec);
-                ++words;
+        if constexpr (SPEC) {
+            if (T.n_energy > 0) {
+                // incident-energy spectrum: [crossings, entrance-cosine sum] per bin and class
+                const int kb = energy_bin<R>(T, E);
+                if (kb >= 0) {
+                    unsigned long long* sp = acc + MIDSX_SCALAR_SLOTS + (size_t(kb) * 4 + cls0) * 2;
+                    count1(sp);
+                    Acc<MX>::cosine(sp + 1, ec);
+                    ++words;
+                }
             }
         }
     }
@@ -529,6 +535,7 @@ struct midsx_gpu_tallies {
     unsigned long long* stats = nullptr;
     int precision = -1;   // precision of the accumulated contents, -1 = empty
     bool pooled = false;  // one pool block starting at `stats`, owned by a request server
+    bool spectra = false; // some surface tally keeps an incident-energy spectrum
 };
 
 namespace {
@@ -1185,6 +1192,7 @@ midsx_status tallies_layout(size_t n_voxels, const midsx_tally_spec* specs, int3
         words += (s.kind == MIDSX_TALLY_SURFACE_BINNED_RECT) ? size_t(s.nu) * s.nv * 8
                                                               : kScalarWords + size_t(d.n_energy) * 8;
         t->host_specs.push_back(d);
+        if (d.n_energy > 0) t->spectra = true;
     }
     t->acc_words = words;
     return MIDSX_OK;
@@ -1359,7 +1367,11 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
         set_last_error("unknown tracking");
         return MIDSX_INVALID_ARG;
     }
-    const bool pool = cfg.scheduler != MIDSX_SCHED_LANES && P.trace == nullptr &&
+    if (P.spectra && (cfg.scheduler == MIDSX_SCHED_POOL || cfg.tracking != MIDSX_TRACK_REFERENCE)) {
+        set_last_error("incident-energy spectra are scored by the lane-parking scheduler with reference tracking");
+        return MIDSX_INVALID_ARG;
+    }
+    const bool pool = cfg.scheduler != MIDSX_SCHED_LANES && P.trace == nullptr && !P.spectra &&
                       (cfg.scheduler == MIDSX_SCHED_POOL || kDefaultScheduler == MIDSX_SCHED_POOL);
     if (cfg.tracking != MIDSX_TRACK_REFERENCE && !pool) {
         set_last_error("background fast and macro-cell tracking run in the photon-pool scheduler only");
@@ -1429,6 +1441,7 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
     P.counter = tallies->stats + kStCount;
     P.total = cfg->n_histories;
     P.trace = trace;
+    P.spectra = tallies->spectra;
     midsx_status st = launch_kernel(tables, P, *cfg, false, stream);
     if (st == MIDSX_OK) tallies->precision = cfg->precision;
     return st;
@@ -1780,6 +1793,7 @@ void batch_params(const midsx_gpu_batch* b, RunParams& P, const unsigned long lo
     P.counter = b->words;
     P.total = total;
     P.epoch = b->words + 1;
+    for (auto* t : b->tallies) P.spectra |= t->spectra;
 }
 
 midsx_status batch_check_precision(midsx_gpu_batch* b, int precision) {
@@ -1955,6 +1969,9 @@ extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precis
                     }
         c.scheduler = MIDSX_SCHED_POOL;
         c.chunk = 0;
+        bool spectra = false;
+        for (auto* t : b->tallies) spectra |= t->spectra;
+        if (!spectra)
         for (int bs : {64, 128, 256})
             for (int ps : {0})
                 for (int rg : {24, 28, 32}) {
@@ -2057,9 +2074,12 @@ midsx_status pack_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_sour
     return MIDSX_OK;
 }
 
+bool tallies_spectra(midsx_tallies_h t) { return t && t->spectra; }
+
 midsx_status launch_packed(midsx_tables_h tables, const void* dev_jobs, int n_jobs,
                            const unsigned long long* dev_prefix, unsigned long long total,
-                           unsigned long long* dev_counter, const midsx_run_config& cfg, cudaStream_t s) {
+                           unsigned long long* dev_counter, const midsx_run_config& cfg, cudaStream_t s,
+                           bool spectra) {
     if (!tables || !dev_jobs || !dev_prefix || !dev_counter || n_jobs < 1 || n_jobs > kMaxBatchJobs)
         return MIDSX_INVALID_ARG;
     if (cfg.precision != MIDSX_PREC_FP64 && cfg.precision != MIDSX_PREC_MIXED) {
@@ -2075,6 +2095,7 @@ midsx_status launch_packed(midsx_tables_h tables, const void* dev_jobs, int n_jo
     P.prefix = dev_prefix;
     P.counter = dev_counter;
     P.total = total;
+    P.spectra = spectra;
     return launch_kernel(tables, P, cfg, true, s);
 }
 

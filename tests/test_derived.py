@@ -262,3 +262,10 @@ def test_gpu_spectrum_mixed_matches_fp64_and_validation():
     tl = M.Tallies(ph, [dict(spec, spectrum=None)], N.DOSE_OFF)
     with pytest.raises(N.MidsxError):
         N.check(N.load().midsx_gpu_fetch_spectrum(tl.handle, 0, None, None, None), "fetch")
+    # spectra are scored by the lane-parking scheduler with reference tracking
+    tl = M.Tallies(ph, [spec], N.DOSE_OFF)
+    for kw in (dict(scheduler="pool"), dict(tracking="background_fast"), dict(tracking="macro_cell")):
+        with pytest.raises(N.MidsxError) as e:
+            M.run(tables, ph, src, tl, 100, seed=1, **kw)
+        assert e.value.status == N.INVALID_ARG, kw
+    M.run(tables, ph, src, tl, 100, seed=1, scheduler="lanes")
