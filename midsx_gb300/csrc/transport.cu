@@ -511,7 +511,8 @@ struct midsx_gpu_phantom {
     uint8_t* ids = nullptr;
     size_t n_voxels = 0;                       // all grids
     DevGrid* extra = nullptr;                  // grids after the first (device)
-    uint32_t* cells = nullptr;                 // macro-cell material masks (device)
+    uint32_t* cells = nullptr;                 // macro-cell material masks (device), built on first use
+    int cell_shift = 3;                        // their edge, 2^cell_shift voxels
     std::vector<midsx_grid_spec> grids;        // every grid's geometry (ids pointers cleared)
     std::vector<DevGrid> host_extra;           // host copy of `extra`
     const midsx_gpu_tables* tables = nullptr;  // the tables its dense material indices refer to
@@ -817,6 +818,7 @@ midsx_status build_cells(midsx_gpu_phantom* p, int shift) {
     }
     cudaFree(p->cells);
     p->cells = cells;
+    p->cell_shift = shift;
     p->G.cells = cells;
     p->G.cell_shift = shift;
     for (int i = 0; i < 3; ++i) p->G.cdims[i] = cdim(p->grids[0].dims[i]);
@@ -902,8 +904,12 @@ midsx_status phantom_create_impl(midsx_tables_h tables, const double* domain, in
         }
         off += n;
     }
+    // the grids after the first (their macro-cell fields are filled when the cells are built)
     bool good = cuda_ok(cudaMemcpy(dlut, lut, 256, cudaMemcpyHostToDevice), "cudaMemcpy") &&
-                cuda_ok(cudaMemset(bad, 0, sizeof(int)), "cudaMemset");
+                cuda_ok(cudaMemset(bad, 0, sizeof(int)), "cudaMemset") &&
+                (extra.empty() || cuda_ok(cudaMemcpy(p->extra, extra.data(), sizeof(DevGrid) * extra.size(),
+                                                     cudaMemcpyHostToDevice),
+                                          "cudaMemcpy"));
     int hbad = 0;
     if (good) {
         remap_kernel<<<tables->sm_count * 8, 256>>>(raw, p->ids, dlut, total, bad);
@@ -937,14 +943,13 @@ midsx_status phantom_create_impl(midsx_tables_h tables, const double* domain, in
     p->grids.assign(grids, grids + n_grids);
     for (auto& gs : p->grids) gs.ids = nullptr;
     p->host_extra = extra;
-    const midsx_status cst = build_cells(p, kCellShiftDefault);
-    if (cst != MIDSX_OK) {
-        midsx_gpu_phantom_destroy(p);
-        return cst;
-    }
+    p->cell_shift = kCellShiftDefault;
     *out = p;
     return MIDSX_OK;
 }
+
+// The macro cells a MIDSX_TRACK_MACRO_CELL launch reads, built on first use.
+midsx_status ensure_cells(midsx_gpu_phantom* p) { return p->cells ? MIDSX_OK : build_cells(p, p->cell_shift); }
 
 }  // namespace
 
@@ -975,6 +980,13 @@ extern "C" midsx_status midsx_gpu_phantom_macro_cells(midsx_phantom_h p, int32_t
     }
     int shift = 0;
     while ((1 << shift) < edge) ++shift;
+    if (!p->ids) {  // not resident: built with this edge when first needed
+        cudaFree(p->cells);
+        p->cells = nullptr;
+        p->G.cells = nullptr;
+        p->cell_shift = shift;
+        return MIDSX_OK;
+    }
     return build_cells(p, shift);
 }
 
@@ -1433,6 +1445,10 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
         return MIDSX_INVALID_ARG;
     }
     if (cfg->n_histories == 0) return MIDSX_OK;
+    if (cfg->tracking == MIDSX_TRACK_MACRO_CELL) {
+        const midsx_status cs = ensure_cells(phantom);
+        if (cs != MIDSX_OK) return cs;
+    }
     RunParams P;
     std::memset(&P, 0, sizeof(P));
     P.T = tables->T;
@@ -1488,39 +1504,49 @@ extern "C" midsx_status midsx_gpu_fetch_stats(midsx_tallies_h t, midsx_run_stats
     return MIDSX_OK;
 }
 
+namespace {
+// Voxel dose records to doubles on the device (the host conversion of fx_signed, term for
+// term): one output array per requested quantity, written with coalesced stores.
+__global__ void dose_convert_kernel(const unsigned long long* rec, int stride, size_t n, int mixed, double* sum,
+                                    double* sumsq, double* count) {
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const unsigned long long* r = rec + i * size_t(stride);
+        if (sum) sum[i] = mixed ? double((long long)r[0]) / kFxEnergy : __longlong_as_double((long long)r[0]);
+        if (sumsq) sumsq[i] = mixed ? double(r[1]) / kFxEnergy2 : __longlong_as_double((long long)r[1]);
+        if (count) count[i] = double(r[2]);
+    }
+}
+}  // namespace
+
+// The conversion runs on the device into stream-ordered scratch, and the doubles go straight
+// into the caller's arrays (a DMA into pinned memory; no host pass over the voxels).
 extern "C" midsx_status midsx_gpu_fetch_dose(midsx_tallies_h t, double* sum, double* sumsq, double* count,
                                              void* stream) {
     if (!t || !t->dose) return MIDSX_INVALID_ARG;
     if ((sumsq || count) && t->dose_stride < 4) return MIDSX_INVALID_ARG;
-    size_t n = t->n_voxels, w = size_t(t->dose_stride);
-    std::vector<unsigned long long> h(n * w);
-    CUDA_TRY(cudaMemcpyAsync(h.data(), t->dose, n * w * 8, cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream)));
-    midsx_status st = wait_stream(stream);
-    if (st != MIDSX_OK) return st;
-    const bool mixed = t->precision == MIDSX_PREC_MIXED;
-    for (size_t i = 0; i < n; ++i) {
-        const unsigned long long* r = &h[i * w];
-        if (sum) {
-            if (mixed) {
-                sum[i] = fx_signed(r[0], kFxEnergy);
-            } else {
-                double d;
-                std::memcpy(&d, &r[0], 8);
-                sum[i] = d;
-            }
-        }
-        if (sumsq) {
-            if (mixed) {
-                sumsq[i] = double(r[1]) / kFxEnergy2;
-            } else {
-                double d;
-                std::memcpy(&d, &r[1], 8);
-                sumsq[i] = d;
-            }
-        }
-        if (count) count[i] = double(r[2]);
+    const size_t n = t->n_voxels;
+    if (n == 0 || (!sum && !sumsq && !count)) return MIDSX_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double* outs[3] = {sum, sumsq, count};
+    double* dev[3] = {nullptr, nullptr, nullptr};
+    bool good = true;
+    for (int k = 0; k < 3 && good; ++k)
+        if (outs[k]) good = cuda_ok(cudaMallocAsync(&dev[k], n * 8, s), "cudaMallocAsync");
+    if (good) {
+        int sms = 0, device = 0;
+        cudaGetDevice(&device);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        dose_convert_kernel<<<std::max(1, sms) * 8, 256, 0, s>>>(t->dose, t->dose_stride, n,
+                                                                t->precision == MIDSX_PREC_MIXED, dev[0], dev[1],
+                                                                dev[2]);
+        good = cuda_ok(cudaGetLastError(), "dose_convert_kernel");
     }
-    return MIDSX_OK;
+    for (int k = 0; k < 3 && good; ++k)
+        if (outs[k]) good = cuda_ok(cudaMemcpyAsync(outs[k], dev[k], n * 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    for (int k = 0; k < 3; ++k)
+        if (dev[k]) cudaFreeAsync(dev[k], s);
+    if (!good) return MIDSX_CUDA_ERROR;
+    return wait_stream(stream);
 }
 
 extern "C" midsx_status midsx_gpu_fetch_scalar(midsx_tallies_h t, int32_t index, double* out, void* stream) {
@@ -1845,6 +1871,12 @@ extern "C" midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const mids
             delete b;
             return cst;
         }
+        // the tracking of the batch's launches is not known yet: the cells exist for any
+        cst = ensure_cells(j.phantom);
+        if (cst != MIDSX_OK) {
+            delete b;
+            return cst;
+        }
         DevJob d;
         std::memset(&d, 0, sizeof(d));
         fill_job(d, j.phantom, j.source, j.tallies, j.seed, j.first_history, j.n_histories);
@@ -2067,6 +2099,8 @@ midsx_status pack_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_sour
         set_last_error("phantom not resident on the device");
         return MIDSX_INVALID_ARG;
     }
+    const midsx_status cs = ensure_cells(phantom);  // the launch's tracking is not known here
+    if (cs != MIDSX_OK) return cs;
     DevJob d;
     std::memset(&d, 0, sizeof(d));
     fill_job(d, phantom, source, tallies, seed, first, n);
