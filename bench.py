@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--serving-requests", type=int, default=120, help="requests at 200/s in the serving leg")
     p.add_argument("--radiography", type=int, default=1, help="run the radiography precision-ablation leg (1/0)")
     p.add_argument("--radiography-histories", type=float, default=1e6, help="histories per precision (radiography)")
+    p.add_argument("--radiography-only", action="store_true",
+                   help="run the radiography precision-ablation leg alone and print its JSON (profiling)")
     return p.parse_args()
 
 
@@ -161,6 +163,13 @@ def main():
         return
     import numpy as np
     import torch
+    if args.radiography_only:
+        from midsx_gb300 import build as B
+        B.build()
+        torch.cuda.set_device(local)
+        if rank == 0:
+            print(json.dumps(radiography_leg(args, np, torch)), flush=True)
+        return
 
     import midsx_gb300 as M
     from midsx_gb300 import build as B, native as N, scenes

@@ -223,7 +223,12 @@ __device__ __forceinline__ void box_span(const V3<R>& p, const V3<R>& d, const V
     }
 }
 
-constexpr int kCellWalkLimit = 4096;  // cells one flight crosses at most (then it ends on a cell face)
+// Cells one flight crosses at most; a longer flight ends on a cell face (through the sliver
+// below) and goes on in the photon's next step.  Short walks keep the lanes of a warp
+// together: 16 against an unbounded walk measured +8 % on the cone-beam dose workload and
+// +10 % on the lead radiography (8^3 cells), and 3.1e8 against 2.8e8 histories/s on the
+// radiography with 4^3 cells.
+constexpr int kCellWalkLimit = 16;
 
 // A flight of the opt-in tracking modes that reaches a face (a grid entered from the
 // background, a grid left, the walk limit) goes on past it for kCutSliver cm against the
