@@ -1,5 +1,7 @@
 // Core.h - umbrella header of the MIDSX C++ API (reference: include/MIDSX/Core.h).
 #pragma once
+#include <iostream>  // the reference's programs use std::cout through this header
+
 #include "Core/computational_domain.h"
 #include "Core/constants.h"
 #include "Core/derived_quantities.h"

@@ -13,11 +13,7 @@
 #include "interaction_data.h"
 #include "surface_quantity_container.h"
 
-#if !defined(EIGEN_WORLD_VERSION) && !defined(MIDSX_NO_EIGEN_ALIAS)
-namespace Eigen {
-using VectorXd = std::vector<double>;
-}
-#endif
+#include "matrix.h"  // Eigen::VectorXd without Eigen
 
 namespace DerivedQuantity {
 // Primary photons (or, cosine-weighted, the sum of their entrance cosines) in the energy

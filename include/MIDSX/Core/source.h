@@ -12,12 +12,14 @@
 #include <vector>
 
 #include "../../midsx_gpu.h"
+#include "matrix.h"
 #include "vec3.h"
 
 namespace SourceHelpers {
 Vec3 angleToUnitDirection(double theta, double phi);
-// Rows of comma-separated numbers (src/MIDSX/Core/source.cpp:11-42).
-std::vector<std::vector<double>> readCSV(const std::string& file);
+// Rows of comma-separated numbers (src/MIDSX/Core/source.cpp:11-42), as a matrix that also
+// converts to rows of numbers.
+midsx::Matrix readCSV(const std::string& file);
 }  // namespace SourceHelpers
 
 struct Photon {

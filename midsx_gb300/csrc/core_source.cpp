@@ -28,7 +28,7 @@ Vec3 SourceHelpers::angleToUnitDirection(double theta, double phi) {
     return {std::sin(theta) * std::cos(phi), std::sin(theta) * std::sin(phi), std::cos(theta)};
 }
 
-std::vector<std::vector<double>> SourceHelpers::readCSV(const std::string& file) {
+midsx::Matrix SourceHelpers::readCSV(const std::string& file) {
     std::string ext = file.size() > 4 ? file.substr(file.size() - 4) : "";
     if (ext != ".csv" && ext != ".txt") throw std::invalid_argument("File is not a csv or txt file");
     std::ifstream in(file);
@@ -43,7 +43,7 @@ std::vector<std::vector<double>> SourceHelpers::readCSV(const std::string& file)
         while (std::getline(ls, cell, ',')) row.push_back(std::stod(cell));
         rows.push_back(row);
     }
-    return rows;
+    return midsx::Matrix(rows);
 }
 
 void EnergySpectrum::describe(midsx_source_spec&) const {

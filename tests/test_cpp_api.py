@@ -223,3 +223,34 @@ def test_cpp_spectrum_air_kerma_program(golden, tmp_path):
     sig = r * math.sqrt((1 - pa) / (n * pa) + (1 - pb) / (n * pb))
     # 0.5 %: the allowance for the two builds' cross-section tables (test_derived.POLY_SYSTEMATIC)
     assert abs(r - ref) < 4 * sig + 0.005 * ref, (r, ref, sig)
+
+
+REFERENCE_ROOT = os.environ.get("MIDSX_REFERENCE_ROOT", "/root/reference")
+REFERENCE_PROGRAMS = ["half_value_layer/hvl_30keV", "half_value_layer/hvl_30kVp", "half_value_layer/hvl_100keV",
+                      "half_value_layer/hvl_100kVp", "lead_attenuation/lead_attenuation", "radiography/radiography",
+                      "radiography/radiography_15_degrees", "CT_w_voxelized_solid/CT_w_voxelized_solid"]
+
+
+@pytest.mark.parametrize("program", REFERENCE_PROGRAMS)
+def test_reference_programs_build_unchanged(program, tmp_path):
+    """The reference's own example programs (cpp_simulations/*.cpp, read where the reference
+    checkout lies, not copied) compile and link against include/MIDSX and the two libraries
+    without a change: the drop-in claim of the C++ API.  They include pybind11's embedding
+    header, so Python's headers and library stand in for the reference's pybind11 submodule."""
+    src = os.path.join(REFERENCE_ROOT, "cpp_simulations", program + ".cpp")
+    if not os.path.exists(src):
+        pytest.skip("reference checkout not present")
+    pybind11 = pytest.importorskip("pybind11")
+    import sysconfig
+    py_inc = sysconfig.get_paths()["include"]
+    if not os.path.exists(os.path.join(py_inc, "Python.h")):
+        pytest.skip("Python headers not present")
+    ver = sysconfig.get_config_var("LDVERSION") or sysconfig.get_config_var("VERSION")
+    libdir = sysconfig.get_config_var("LIBDIR")
+    out = tmp_path / os.path.basename(program)
+    cmd = ["g++", "-std=c++17", "-fopenmp", "-O0", "-I", os.path.join(build.ROOT, "include"),
+           "-I", pybind11.get_include(), "-I", py_inc, src, "-o", str(out),
+           "-L", LIB, "-lmidsx_core", "-lmidsx_gb300", "-L", libdir, "-lpython" + ver]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert out.exists()
