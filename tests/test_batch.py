@@ -116,3 +116,21 @@ def test_batch_rejects_mismatched_tables(setup):
     with pytest.raises(N.MidsxError) as e:
         M.Batch(tables, [(ph, src, tl, 1, 0, 10)])
     assert e.value.status == N.INVALID_ARG
+
+
+@pytest.mark.parametrize("tracking", ["background_fast", "macro_cell"])
+def test_batch_opt_in_tracking_equals_single_runs(setup, tracking):
+    """The opt-in tracking modes in batched launches (per-job geometry and macro cells from
+    the job records): each job equals its single run with the same mode, bit for bit."""
+    tables, jobs = setup
+    objs = [make(tables, sc) for sc in jobs]
+    batch = M.Batch(tables, [(ph, src, tl, 40 + j, 0, sc.n_histories)
+                             for j, (sc, (ph, src, tl)) in enumerate(zip(jobs, objs))])
+    batch.run("mixed", tracking=tracking)
+    for j, sc in enumerate(jobs):
+        ph, src, tl = make(tables, sc)
+        M.run(tables, ph, src, tl, sc.n_histories, seed=40 + j, precision="mixed", tracking=tracking)
+        a, b = results(objs[j][2]), results(tl)
+        for x, y in zip(a[:3], b[:3]):
+            np.testing.assert_array_equal(x, y)
+        assert a[3]["steps"] == b[3]["steps"] and a[3]["histories"] == sc.n_histories

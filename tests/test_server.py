@@ -34,10 +34,10 @@ def env():
     return tabs, flat, sources
 
 
-def alone(tables, sc, src, n, seed, first, precision):
+def alone(tables, sc, src, n, seed, first, precision, tracking="reference"):
     ph = M.Phantom(tables, sc.domain, sc.spacing, sc.origin, sc.ids, sc.background)
     tl = M.Tallies(ph, sc.specs, sc.dose_mode)
-    M.run(tables, ph, src, tl, n, seed=seed, first=first, precision=precision)
+    M.run(tables, ph, src, tl, n, seed=seed, first=first, precision=precision, tracking=tracking)
     return read(tl, sc)
 
 
@@ -109,6 +109,24 @@ def test_results_same_alone_and_in_the_mix(env):
         srv.release(ids[k])
     st = srv.stats()
     assert st["bytes_in_use"] == st["resident_phantom_bytes"]
+    srv.close()
+
+
+def test_macro_cell_tracking_in_the_mix(env):
+    """A server launching with MIDSX_TRACK_MACRO_CELL: the requests' phantoms get their
+    macro cells when packed, and every request equals its single run with that tracking."""
+    tabs, flat, sources = env
+    srv = M.Server(tabs[0], launch_histories=30_000, in_flight=2, tracking="macro_cell")
+    pids = register(srv, flat, tabs)
+    plan = [(j % len(flat), 20_000 + 5_000 * j, 300 + j, 17 * j) for j in range(6)]
+    ids = [srv.submit(pids[j], sources[j], n, seed, first, "mixed", flat[j].specs, flat[j].dose_mode)
+           for j, n, seed, first in plan]
+    for k, (j, n, seed, first) in enumerate(plan):
+        srv.wait(ids[k], timeout=300)
+        got = read(srv.tallies(ids[k]), flat[j])
+        same(got, alone(tabs[j], flat[j], sources[j], n, seed, first, "mixed", "macro_cell"), exact=True)
+        srv.release(ids[k])
+    assert srv.stats()["failed"] == 0
     srv.close()
 
 
