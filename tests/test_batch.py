@@ -134,3 +134,33 @@ def test_batch_opt_in_tracking_equals_single_runs(setup, tracking):
         for x, y in zip(a[:3], b[:3]):
             np.testing.assert_array_equal(x, y)
         assert a[3]["steps"] == b[3]["steps"] and a[3]["histories"] == sc.n_histories
+
+
+def test_batch_with_spectrum_tallies_equals_single_runs(setup):
+    """Jobs whose tallies keep incident-energy spectra run on the lane-parking kernel in a
+    batch as alone (the photon pool is refused for them); each equals its single run."""
+    tables, jobs = setup
+    objs = []
+    specs = []
+    for sc in jobs[:2]:
+        ext = [n * h for n, h in zip(sc.ids.shape[::-1], sc.spacing)]
+        z = sc.origin[2] + ext[2]
+        spec = dict(kind="rect", corner=(sc.origin[0], sc.origin[1], z), edge1=(ext[0], 0, 0), edge2=(0, ext[1], 0),
+                    spectrum=(0.0, 2000.0, 80))
+        specs.append(spec)
+        ph = M.Phantom(tables, sc.domain, sc.spacing, sc.origin, sc.ids, sc.background)
+        objs.append((ph, M.Source(**sc.source), M.Tallies(ph, [spec], sc.dose_mode)))
+    batch = M.Batch(tables, [(ph, src, tl, 70 + j, 0, sc.n_histories)
+                             for j, (sc, (ph, src, tl)) in enumerate(zip(jobs[:2], objs))])
+    with pytest.raises(N.MidsxError):
+        batch.run("mixed", scheduler="pool")
+    batch.run("mixed")
+    for j, sc in enumerate(jobs[:2]):
+        ph = M.Phantom(tables, sc.domain, sc.spacing, sc.origin, sc.ids, sc.background)
+        tl = M.Tallies(ph, [specs[j]], sc.dose_mode)
+        M.run(tables, ph, M.Source(**sc.source), tl, sc.n_histories, seed=70 + j, precision="mixed")
+        a, b = objs[j][2].spectrum(0), tl.spectrum(0)
+        assert a[0].sum() > 0
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
+        np.testing.assert_array_equal(objs[j][2].dose()["sum"], tl.dose()["sum"])
