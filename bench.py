@@ -125,6 +125,23 @@ def dist_setup():
     return world, rank, local, dist
 
 
+def replica_first(rank, i, n):
+    """First history id of step i on rank `rank`: replicas take disjoint history ranges of
+    the same Philox key (rank r owns ids [r * 2^40, (r + 1) * 2^40))."""
+    return (rank << 40) + i * n
+
+
+def job_rate(dist, world, steps, n_hist, total_s, device="cuda"):
+    """(whole-job histories/s, the slowest rank's time): every rank ran `steps` steps of
+    n_hist histories in total_s seconds; the job's time is the maximum over ranks."""
+    if dist:
+        import torch
+        t = torch.tensor([total_s], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    return world * steps * n_hist / total_s, total_s
+
+
 def reference_arm(args, world, rank):
     """CPU restatement of the reference transport, all host threads, bounded samples."""
     if rank != 0:
@@ -184,7 +201,7 @@ def main():
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
-    base = rank << 40
+    base = replica_first(rank, 0, 0)
 
     def step(i, precision="mixed", n=N_hist, events=None):
         flush.zero_()
@@ -193,7 +210,7 @@ def main():
         tl.reset(sptr)
         if events:
             events[1].record(stream)
-        M.run(tables, ph, src, tl, n, seed=1, first=base + i * n, precision=precision, stream=sptr)
+        M.run(tables, ph, src, tl, n, seed=1, first=replica_first(rank, i, n), precision=precision, stream=sptr)
         if events:
             events[2].record(stream)
 
@@ -215,12 +232,7 @@ def main():
     clk = clocks.stop()
     step_ms = [e[0].elapsed_time(e[2]) for e in evs]
     kern_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    total_s = sum(step_ms) / 1e3
-    if dist:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * args.steps * N_hist / total_s
+    value, total_s = job_rate(dist, world, args.steps, N_hist, sum(step_ms) / 1e3)
     st = tl.stats()
     result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
