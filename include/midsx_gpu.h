@@ -305,13 +305,15 @@ typedef enum midsx_tracking {
 } midsx_tracking;
 /* MACRO_CELL adds local majorants inside the grids to BACKGROUND_FAST: every grid is split
  * into cells of MIDSX_MACRO_CELL^3 voxels (midsx_gpu_phantom_macro_cells changes the edge),
- * each with the set of materials it holds (built with the phantom).  A flight inside a grid draws one optical depth -ln U and spends it cell
+ * each with the set of materials it holds.  A flight inside a grid draws one optical depth -ln U and spends it cell
  * by cell along the ray, each cell's majorant being the largest attenuation among its own
  * materials at the photon's energy; where the depth runs out a voxel is fetched and the
  * collision is real with probability mu(voxel) / mu(cell).  A flight that leaves its grid
  * ends on the grid's face.  Unbiased, statistically equal to REFERENCE; photon pool only.
  * Where grids overlap, the cells of a later grid that meet an earlier grid's box take every
- * material of the tables (the first grid owns the overlap). */
+ * material of the tables (the first grid owns the overlap).  A phantom's cells are built on
+ * its first MACRO_CELL run (or when it joins a batch or a server launch): that call
+ * synchronises the device once. */
 #define MIDSX_MACRO_CELL 8
 
 typedef struct midsx_run_config {
