@@ -295,7 +295,9 @@ typedef enum midsx_scheduler {
  * (src/MIDSX/Core/physics_engine.cpp:28-79, interaction_data.cpp:42-73).  BACKGROUND_FAST:
  * outside every voxel grid the medium is the background material alone, so its own
  * attenuation is an exact majorant there: a flight that starts in the background is sampled
- * with it and ends at a real collision, at the first grid it enters, or out of the domain.
+ * with it and ends at a real collision, out of the domain, or - at the first grid it enters -
+ * 1e-4 cm inside that grid, that last stretch against the global majorant (so that no flight
+ * ends on a face where a tally plane may lie).
  * Unbiased (same distributions) but not the reference's random-number use, so results agree
  * with REFERENCE statistically, not history by history.  Photon-pool scheduler only. */
 typedef enum midsx_tracking {
@@ -305,15 +307,17 @@ typedef enum midsx_tracking {
 } midsx_tracking;
 /* MACRO_CELL adds local majorants inside the grids to BACKGROUND_FAST: every grid is split
  * into cells of MIDSX_MACRO_CELL^3 voxels (midsx_gpu_phantom_macro_cells changes the edge),
- * each with the set of materials it holds.  A flight inside a grid draws one optical depth -ln U and spends it cell
- * by cell along the ray, each cell's majorant being the largest attenuation among its own
- * materials at the photon's energy; where the depth runs out a voxel is fetched and the
- * collision is real with probability mu(voxel) / mu(cell).  A flight that leaves its grid
- * ends on the grid's face.  Unbiased, statistically equal to REFERENCE; photon pool only.
- * Where grids overlap, the cells of a later grid that meet an earlier grid's box take every
- * material of the tables (the first grid owns the overlap).  A phantom's cells are built on
- * its first MACRO_CELL run (or when it joins a batch or a server launch): that call
- * synchronises the device once. */
+ * each with the set of materials it holds.  A flight inside a grid draws one optical depth
+ * -ln U and spends it cell by cell along the ray, a cell's majorant being the largest
+ * attenuation among its own materials at the photon's energy; where the depth runs out a
+ * voxel is fetched and the collision is real with probability mu(voxel) / mu(cell).  A flight
+ * that reaches its grid's face (or crosses 16 cells) goes on for 1e-4 cm past that face
+ * against the global majorant and ends there unless it collides; the photon continues in its
+ * next step.  Unbiased, statistically equal to REFERENCE; photon pool only.  Where grids
+ * overlap, the cells of a later grid that meet an earlier grid's box take every material of
+ * the tables (the first grid owns the overlap).  A phantom's cells are built on its first
+ * MACRO_CELL run (or when it joins a batch or a server launch): that call synchronises the
+ * device once. */
 #define MIDSX_MACRO_CELL 8
 
 typedef struct midsx_run_config {
