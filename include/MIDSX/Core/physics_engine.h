@@ -39,6 +39,13 @@ public:
     // first history id of the next run.
     void setPrecision(midsx_precision p) { precision_ = p; }
     void setSeed(uint64_t seed) { seed_ = seed; }
+    // Opt-in flight sampling (midsx_tracking; the reference's global-majorant Woodcock
+    // tracking by default) and the macro-cell edge of MIDSX_TRACK_MACRO_CELL (a power of two,
+    // 1..64 voxels; applied at the next run).  Spectrum tallies need the default tracking:
+    // with another tracking set before the first run, IncidentEnergy tallies get no default
+    // spectrum (DerivedQuantity then throws).
+    void setTracking(midsx_tracking t) { tracking_ = t; }
+    void setMacroCellEdge(int edge) { macro_edge_ = edge; }
     uint64_t nextHistoryId() const { return next_history_; }
     // Transports n histories from `source` into the engine's tallies.  Used by runSimulation.
     double run(PhotonSource& source, uint64_t n_photons);
@@ -52,6 +59,9 @@ private:
     std::vector<std::unique_ptr<SurfaceTally>> surface_tallies_;
     std::unique_ptr<Device> dev_;
     midsx_precision precision_ = MIDSX_PREC_MIXED;
+    midsx_tracking tracking_ = MIDSX_TRACK_REFERENCE;
+    int macro_edge_ = 0;  // 0: the phantom's own (MIDSX_MACRO_CELL)
+    int macro_edge_applied_ = 0;
     uint64_t seed_ = 1;
     uint64_t next_history_ = 0;
     midsx_run_stats stats_{};

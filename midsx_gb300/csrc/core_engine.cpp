@@ -111,7 +111,8 @@ void PhysicsEngine::ensureDevice(const midsx_source_spec& first_source) {
     for (auto& t : surface_tallies_) {
         midsx_tally_spec s = t->describe();
         // a disc or rectangle measuring IncidentEnergy keeps a spectrum for DerivedQuantity
-        if (s.kind != MIDSX_TALLY_SURFACE_BINNED_RECT && !t->hasEnergyBins() &&
+        // (with the reference tracking, which scores spectra)
+        if (s.kind != MIDSX_TALLY_SURFACE_BINNED_RECT && !t->hasEnergyBins() && tracking_ == MIDSX_TRACK_REFERENCE &&
             t->getSurfaceQuantityContainer().getVectorQuantities().count(VectorSurfaceQuantityType::IncidentEnergy))
             default_energy_bins(first_source, s);
         specs.push_back(s);
@@ -127,11 +128,16 @@ void PhysicsEngine::ensureDevice(const midsx_source_spec& first_source) {
 double PhysicsEngine::run(PhotonSource& source, uint64_t n_photons) {
     midsx_source_spec spec = source.describe();
     ensureDevice(spec);
+    if (macro_edge_ != 0 && macro_edge_ != macro_edge_applied_) {
+        check(midsx_gpu_phantom_macro_cells(dev_->phantom, macro_edge_), "midsx_gpu_phantom_macro_cells");
+        macro_edge_applied_ = macro_edge_;
+    }
     midsx_source_h src = nullptr;
     check(midsx_gpu_source_create(&spec, &src), "midsx_gpu_source_create");
     midsx_run_config cfg;
     std::memset(&cfg, 0, sizeof(cfg));
     cfg.precision = precision_;
+    cfg.tracking = tracking_;
     cfg.seed = seed_;
     cfg.first_history = next_history_;
     cfg.n_histories = n_photons;

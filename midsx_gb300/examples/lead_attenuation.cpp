@@ -8,6 +8,7 @@
 //
 //   lead_attenuation <scene.json> <photons> <seed> <precision 0=FP64|1=mixed> <energy_eV>
 //                    <scin_x> <scin_y> <scin_z> <scin_dx> <scin_dy> <scin_dz>
+//                    [tracking 0=reference|1=background fast|2=macro cells [cell edge]]
 //
 // The reference runs 661.7 keV (Cs-137); the mixed form takes energies up to 262 keV, so the
 // energy is an argument.  The interaction tables are built up to max(150 keV, energy).
@@ -40,6 +41,8 @@ int main(int argc, char** argv) {
         PhysicsEngine engine(domain, data);
         engine.setPrecision(precision ? MIDSX_PREC_MIXED : MIDSX_PREC_FP64);
         engine.setSeed(seed);
+        if (argc > 12) engine.setTracking(static_cast<midsx_tracking>(std::atoi(argv[12])));
+        if (argc > 13) engine.setMacroCellEdge(std::atoi(argv[13]));
 
         PhotonSource source(std::make_unique<MonoenergeticSpectrum>(energy),
                             std::make_unique<RectangularIsotropicDirectionality>(

@@ -188,6 +188,50 @@ def test_cpp_multi_grid_program_equals_python_api(tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tracking,edge", [(1, 0), (2, 4)])
+def test_cpp_opt_in_tracking_equals_python_api(tracking, edge, tmp_path):
+    """PhysicsEngine::setTracking / setMacroCellEdge: the lead-attenuation program with
+    background fast or macro-cell tracking equals the Python API with the same mode on the
+    same streams, bit for bit in the mixed form."""
+    from midsx_gb300 import native as N
+    from midsx_gb300 import scenes
+    # a lead block half-way that shadows part of a water scintillator
+    lead = np.full((35, 15, 5), scenes.LEAD, dtype=np.uint8)
+    scin = np.full((30, 30, 10), scenes.WATER, dtype=np.uint8)
+    grids = [(lead, (0.1, 0.1, 0.1), (3.0, 0.5, 0.5)), (scin, (0.1, 0.1, 0.1), (6.0, 0.5, 0.5))]
+    names = ["lead.nii", "scin.nii"]
+    for (ids, _, _), name in zip(grids, names):
+        write_nifti(str(tmp_path / name), ids, (1.0, 1.0, 1.0))
+    dim = (7.2, 4.0, 4.0)
+    js = tmp_path / "scene.json"
+    entries = ", ".join('{"file_path": "%s", "origin": [%g, %g, %g]}' % (nm, *g[2]) for nm, g in zip(names, grids))
+    js.write_text('{"dim_space": [%g, %g, %g], "background_material_name": "Air, Dry (near sea level)", '
+                  '"voxel_grids": [%s]}' % (*dim, entries))
+    n, seed, energy = 100_000, 3, 80e3
+    scin_o, scin_s = (6.0, 0.5, 0.5), (1.0, 3.0, 3.0)
+    r = subprocess.run([exe("lead_attenuation"), str(js), str(n), str(seed), "1", str(energy), *map(str, scin_o),
+                        *map(str, scin_s), str(tracking), str(edge)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    out = parse(r.stdout)
+    tables = M.Tables([scenes.AIR, scenes.LEAD, scenes.WATER], e_max=150e3)
+    ph = M.Phantom.from_grids(tables, dim, scenes.AIR, grids)
+    if edge:
+        ph.macro_cells(edge)
+    src = M.Source(position=(0, dim[1] / 2, dim[2] / 2), direction=("rect", (10, 0, 0), (0, dim[1], 0), (0, 0, dim[2])),
+                   energy=energy)
+    spec = dict(kind="cuboid", min=scin_o, max=tuple(a + b for a, b in zip(scin_o, scin_s)))
+    tl = M.Tallies(ph, [spec], N.DOSE_FULL)
+    M.run(tables, ph, src, tl, n, seed=seed, first=0, precision="mixed",
+          tracking=["reference", "background_fast", "macro_cell"][tracking])
+    sc = tl.scalar(0)
+    assert float(out["energy_deposition"][0][0]) == pytest.approx(sum(sc[1 + 3 * c] for c in range(4)), rel=1e-12)
+    dose = tl.dose()["sum"]
+    for k in range(2):
+        assert float(out["grid_deposit"][k][1]) == pytest.approx(dose[k].sum(), rel=1e-12), k
+    assert dose[0].sum() > 0 and dose[1].sum() > 0
+
+
+@pytest.mark.gpu
 def test_cpp_spectrum_air_kerma_program(golden, tmp_path):
     """The reference's hvl_30kVp.cpp form: a polyenergetic source read from a spectrum CSV
     and DerivedQuantity::getPrimarySpectrumAirKerma over the spectrum files' midpoints.  The
