@@ -191,8 +191,12 @@ def main():
     import midsx_gb300 as M
     from midsx_gb300 import build as B, native as N, scenes
 
-    B.build()
     torch.cuda.set_device(local)
+    # one rank per node compiles (in-tree objects and libraries); the others wait for it
+    if local == 0:
+        B.build()
+    if dist:
+        dist.barrier()
     N_hist = int(args.histories)
     t0 = time.time()
     sc = scenes.cone_beam_dose(n_histories=N_hist)
