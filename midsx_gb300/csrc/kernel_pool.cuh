@@ -19,6 +19,15 @@
 // list are all empty after the launch's histories are handed out.
 
 constexpr int kPoolSlots = 64;        // photon slots per warp
+// Woodcock steps a lane takes per pass of the warp loop before the pool's bookkeeping
+// (ready and event lists, ballots) runs, by tracking mode.  Reference tracking: 2 against 1
+// measured +5.5 to +10 % on the cone-beam dose workload (3, 4 and 6 were slower than 1).
+// The opt-in modes' steps are long (a background flight, a cell walk) and lose 8-9 % with 2.
+// A photon that parks ends its pass early.
+template <int TRACK>
+__host__ __device__ constexpr int steps_per_pass() {
+    return TRACK == MIDSX_TRACK_REFERENCE ? 2 : 1;
+}
 constexpr uint32_t kKindFlight = 0u;  // slot kinds (meta bits 30-31)
 constexpr uint32_t kKindCollide = 1u;
 constexpr uint32_t kKindStart = 2u;
@@ -228,110 +237,112 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         }
         if (__ballot_sync(FULL, cur >= 0) == 0u && rdy_top == 0 && ev_top == 0) break;
         uint32_t park = kKindFlight;
-        bool segment = false;  // the step's segment goes to the tallies (escape or delta step)
-        if (cur >= 0) {
-            // one Woodcock step: getFreePath, move, domain test, voxel fetch, isDeltaScatter
-            const Geo<R>& g = MULTI ? s_geo[job] : g0;
-            unsigned long long* st = s_stats + job * kStCount;
-            if (steps >= uint32_t(P.max_steps)) {
-                stat_add(st, kStStepCap, 1);
-                park = kKindStart;
-            } else {
-                ++steps;
-                uint64_t w1, w2;
-                rng.next_pair64(w1, w2);
-                // MIDSX_TRACK_BACKGROUND_FAST: a photon known to be in the background (vox == -1
-                // after its last voxel lookup) flies against the background's own attenuation,
-                // exact there, up to the first grid it would enter
-                // MIDSX_TRACK_MACRO_CELL: any other photon spends one optical depth through the
-                // macro cells of the grid it is in.  fl: -1 a reference step; 0 a tentative
-                // collision against the cell majorant mu_c; 1 a flight that ends, without
-                // interaction, kCutSliver past a face; 2 a tentative collision in that sliver
-                // (against the global majorant); 3 a background collision (always real)
-                int fl = -1;
-                R mu_c = R(0);
-                if (fast_mode) {
-                    R tau, tau_rem = R(0), lim = R(INFINITY);
-                    if constexpr (MX)
-                        tau = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f);
-                    else
-                        tau = -log_(to_uniform(w1, R(0)));
-                    bool bg = vox == -1;
-                    if (macro_mode && !bg) {
-                        fl = cell_flight<R, MX>(g, MULTI ? P.jobs[job].G : P.job0.G, S.mu + cur, ns, pos, dir, tau,
-                                                s, mu_c, tau_rem);
-                        bg = fl == 2;
-                    }
-                    if (bg) {
-                        const R mu_bg = S.mu[g.bg * ns + cur];
-                        s = tau / mu_bg;
-                        lim = grid_entry<R, MX>(g, pos, dir);
-                        fl = 3;
-                        if (s > lim) {
-                            tau_rem = tau - mu_bg * lim;
-                            s = lim;
-                            fl = 1;
-                        }
-                    }
-                    if (fl == 1) {
-                        const R past = tau_rem * inv_mu_max;
-                        if (past < R(kCutSliver)) {
-                            s += past;
-                            fl = 2;
-                        } else {
-                            s += R(kCutSliver);
-                        }
-                    }
-                }
-                if (fl >= 0) {
-                    // s from the flight above
-                } else if constexpr (MX) {
-                    s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) * inv_mu_max;
-                } else {
-                    s = -log_(to_uniform(w1, R(0))) / mu_max;
-                }
-                p0 = pos;
-                pos = {pos.x + s * dir.x, pos.y + s * dir.y, pos.z + s * dir.z};
-                if (!(pos.x >= R(0) && pos.x <= g.dom.x && pos.y >= R(0) && pos.y <= g.dom.y && pos.z >= R(0) &&
-                      pos.z <= g.dom.z)) {
-                    stat_add(st, kStEscE, fx_stat(E));
-                    segment = true;
+        for (int pass = 0; pass < steps_per_pass<TRACK>() && park == kKindFlight && cur >= 0; ++pass) {
+            bool segment = false;  // the step's segment goes to the tallies (escape or delta step)
+            if (cur >= 0) {
+                // one Woodcock step: getFreePath, move, domain test, voxel fetch, isDeltaScatter
+                const Geo<R>& g = MULTI ? s_geo[job] : g0;
+                unsigned long long* st = s_stats + job * kStCount;
+                if (steps >= uint32_t(P.max_steps)) {
+                    stat_add(st, kStStepCap, 1);
                     park = kKindStart;
-                } else if (fl == 3) {
-                    mat = g.bg;
-                    vox = -1;
-                    park = kKindCollide;  // every background collision is real
-                } else if (fl == 1) {
-                    // past a face, no interaction: the next flight finds its region from here
-                    // (BACKGROUND_FAST: a reference step, valid everywhere)
-                    vox = -2;
-                    segment = true;
-                } else if (fl == 0) {
-                    // real with probability mu(voxel) / mu(cell); a voxel met across a cell face
-                    // by rounding, with a larger attenuation than the cell's, interacts
-                    locate<R, MX>(g, pos, vox, mat, fetches, st);
-                    const R mm = S.mu[mat * ns + cur];
-                    if (to_uniform(w2, R(0)) * mu_c < mu_c - mm)
-                        segment = true;
-                    else
-                        park = kKindCollide;
                 } else {
-                    locate<R, MX>(g, pos, vox, mat, fetches, st);
-                    if (to_uniform(w2, R(0)) < S.thr[mat * ns + cur])
+                    ++steps;
+                    uint64_t w1, w2;
+                    rng.next_pair64(w1, w2);
+                    // MIDSX_TRACK_BACKGROUND_FAST: a photon known to be in the background (vox == -1
+                    // after its last voxel lookup) flies against the background's own attenuation,
+                    // exact there, up to the first grid it would enter
+                    // MIDSX_TRACK_MACRO_CELL: any other photon spends one optical depth through the
+                    // macro cells of the grid it is in.  fl: -1 a reference step; 0 a tentative
+                    // collision against the cell majorant mu_c; 1 a flight that ends, without
+                    // interaction, kCutSliver past a face; 2 a tentative collision in that sliver
+                    // (against the global majorant); 3 a background collision (always real)
+                    int fl = -1;
+                    R mu_c = R(0);
+                    if (fast_mode) {
+                        R tau, tau_rem = R(0), lim = R(INFINITY);
+                        if constexpr (MX)
+                            tau = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f);
+                        else
+                            tau = -log_(to_uniform(w1, R(0)));
+                        bool bg = vox == -1;
+                        if (macro_mode && !bg) {
+                            fl = cell_flight<R, MX>(g, MULTI ? P.jobs[job].G : P.job0.G, S.mu + cur, ns, pos, dir, tau,
+                                                    s, mu_c, tau_rem);
+                            bg = fl == 2;
+                        }
+                        if (bg) {
+                            const R mu_bg = S.mu[g.bg * ns + cur];
+                            s = tau / mu_bg;
+                            lim = grid_entry<R, MX>(g, pos, dir);
+                            fl = 3;
+                            if (s > lim) {
+                                tau_rem = tau - mu_bg * lim;
+                                s = lim;
+                                fl = 1;
+                            }
+                        }
+                        if (fl == 1) {
+                            const R past = tau_rem * inv_mu_max;
+                            if (past < R(kCutSliver)) {
+                                s += past;
+                                fl = 2;
+                            } else {
+                                s += R(kCutSliver);
+                            }
+                        }
+                    }
+                    if (fl >= 0) {
+                        // s from the flight above
+                    } else if constexpr (MX) {
+                        s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) * inv_mu_max;
+                    } else {
+                        s = -log_(to_uniform(w1, R(0))) / mu_max;
+                    }
+                    p0 = pos;
+                    pos = {pos.x + s * dir.x, pos.y + s * dir.y, pos.z + s * dir.z};
+                    if (!(pos.x >= R(0) && pos.x <= g.dom.x && pos.y >= R(0) && pos.y <= g.dom.y && pos.z >= R(0) &&
+                          pos.z <= g.dom.z)) {
+                        stat_add(st, kStEscE, fx_stat(E));
                         segment = true;
-                    else
-                        park = kKindCollide;  // a real collision
+                        park = kKindStart;
+                    } else if (fl == 3) {
+                        mat = g.bg;
+                        vox = -1;
+                        park = kKindCollide;  // every background collision is real
+                    } else if (fl == 1) {
+                        // past a face, no interaction: the next flight finds its region from here
+                        // (BACKGROUND_FAST: a reference step, valid everywhere)
+                        vox = -2;
+                        segment = true;
+                    } else if (fl == 0) {
+                        // real with probability mu(voxel) / mu(cell); a voxel met across a cell face
+                        // by rounding, with a larger attenuation than the cell's, interacts
+                        locate<R, MX>(g, pos, vox, mat, fetches, st);
+                        const R mm = S.mu[mat * ns + cur];
+                        if (to_uniform(w2, R(0)) * mu_c < mu_c - mm)
+                            segment = true;
+                        else
+                            park = kKindCollide;
+                    } else {
+                        locate<R, MX>(g, pos, vox, mat, fetches, st);
+                        if (to_uniform(w2, R(0)) < S.thr[mat * ns + cur])
+                            segment = true;
+                        else
+                            park = kKindCollide;  // a real collision
+                    }
                 }
             }
-        }
-        // surface and volume tallies see every step that does not interact, the last (escaping)
-        // one included (physics_engine.cpp:48-49).  Scored per lane: nearly every step runs
-        // this and almost none touches a tally, so the warp-collective form (used for the
-        // collisions below) measured 3 % slower on the cone-beam dose workload and 29 % slower
-        // on the radiography workload.
-        if (segment && ntal > 0)
-            score_tallies<R, MX, false>(MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, dir, s, E,
-                                 scatter_class(n_coh, n_incoh), 0, false, R(0), words);
+            // surface and volume tallies see every step that does not interact, the last (escaping)
+            // one included (physics_engine.cpp:48-49).  Scored per lane: nearly every step runs
+            // this and almost none touches a tally, so the warp-collective form (used for the
+            // collisions below) measured 3 % slower on the cone-beam dose workload and 29 % slower
+            // on the radiography workload.
+            if (segment && ntal > 0)
+                score_tallies<R, MX, false>(MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, dir, s, E,
+                                     scatter_class(n_coh, n_incoh), 0, false, R(0), words);
+        }  // pass
         if (cur >= 0 && park == kKindStart) end_history();
         // photons that need an event go to the event list
         {
