@@ -378,7 +378,8 @@ midsx_status midsx_gpu_fetch_spectrum(midsx_tallies_h t, int32_t index, double* 
                                       void* stream);
 
 /* One call from host memory to host memory: uploads the phantom ids, runs, and reads the
- * dose sum and statistics back (the end-to-end form used by the C++ runSimulation). */
+ * dose sum and statistics back; nothing stays on the device.  (The C++ PhysicsEngine keeps
+ * its tables, phantom and tallies resident across runs instead.) */
 midsx_status midsx_gpu_run_host(midsx_tables_h tables, const midsx_geometry_spec* geom,
                                 const uint8_t* ids, const midsx_source_spec* source,
                                 const midsx_tally_spec* specs, int32_t n_specs, int32_t dose_mode,
