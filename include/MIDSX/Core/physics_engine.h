@@ -41,9 +41,7 @@ public:
     void setSeed(uint64_t seed) { seed_ = seed; }
     // Opt-in flight sampling (midsx_tracking; the reference's global-majorant Woodcock
     // tracking by default) and the macro-cell edge of MIDSX_TRACK_MACRO_CELL (a power of two,
-    // 1..64 voxels; applied at the next run).  Spectrum tallies need the default tracking:
-    // with another tracking set before the first run, IncidentEnergy tallies get no default
-    // spectrum (DerivedQuantity then throws).
+    // 1..64 voxels; applied at the next run).
     void setTracking(midsx_tracking t) { tracking_ = t; }
     void setMacroCellEdge(int edge) { macro_edge_ = edge; }
     uint64_t nextHistoryId() const { return next_history_; }

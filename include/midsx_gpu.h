@@ -245,8 +245,9 @@ midsx_status midsx_gpu_source_destroy(midsx_source_h s);
  * and the sum of their entrance cosines.  It replaces the raw IncidentEnergy/EntranceCosine
  * vectors that DerivedQuantity::getPrimaryFluence scans (src/MIDSX/Core/derived_quantities.cpp:
  * 3-45): with bins centred on the source's energies every primary photon sits at a bin centre.
- * Launches with a spectrum tally run the lane-parking scheduler with reference tracking
- * (MIDSX_SCHED_POOL or another tracking is refused with MIDSX_INVALID_ARG).
+ * Batched launches (midsx_gpu_batch_*, the request server) with a spectrum tally run the
+ * lane-parking scheduler with reference tracking (MIDSX_SCHED_POOL or another tracking is
+ * refused with MIDSX_INVALID_ARG there); single runs take any scheduler and tracking.
  * The voxel dose tally (per grid voxel: deposit count, sum, sum of squares - the summary
  * of the reference's Voxel::dose VectorValue) is enabled by dose_mode. */
 typedef enum midsx_tally_kind {

@@ -111,8 +111,7 @@ void PhysicsEngine::ensureDevice(const midsx_source_spec& first_source) {
     for (auto& t : surface_tallies_) {
         midsx_tally_spec s = t->describe();
         // a disc or rectangle measuring IncidentEnergy keeps a spectrum for DerivedQuantity
-        // (with the reference tracking, which scores spectra)
-        if (s.kind != MIDSX_TALLY_SURFACE_BINNED_RECT && !t->hasEnergyBins() && tracking_ == MIDSX_TRACK_REFERENCE &&
+        if (s.kind != MIDSX_TALLY_SURFACE_BINNED_RECT && !t->hasEnergyBins() &&
             t->getSurfaceQuantityContainer().getVectorQuantities().count(VectorSurfaceQuantityType::IncidentEnergy))
             default_energy_bins(first_source, s);
         specs.push_back(s);

@@ -76,10 +76,12 @@ __host__ __device__ inline size_t pool_smem(int n_jobs, bool multi, int n_materi
 }
 
 // TRACK = midsx_tracking, each a kernel of its own (compiled into one kernel with the
-// reference tracking, the background fast path's code cost the reference path 8 %).  Batched
+// reference tracking, the background fast path's code cost the reference path 8 %).  SPEC:
+// the launch keeps incident-energy spectra (a kernel of its own too: the spectrum code cost
+// tally-free launches 5 %).  Batched
 // launches take blocks of up to 256 threads: their per-job counters and geometry in shared
 // memory (~16 KB for 64 jobs) are then shared by twice the photon slots.
-template <typename R, bool MULTI, int TRACK>
+template <typename R, bool MULTI, int TRACK, bool SPEC = false>
 __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3 : 6) : (MULTI ? 2 : 4))
     transport_pool_kernel(const RunParams P) {
     constexpr bool MX = sizeof(R) == 4;
@@ -340,7 +342,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
             // collisions below) measured 3 % slower on the cone-beam dose workload and 29 % slower
             // on the radiography workload.
             if (segment && ntal > 0)
-                score_tallies<R, MX, false>(MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, dir, s, E,
+                score_tallies<R, MX, SPEC>(MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, dir, s, E,
                                      scatter_class(n_coh, n_incoh), 0, false, R(0), words);
         }  // pass
         if (cur >= 0 && park == kKindStart) end_history();
@@ -452,7 +454,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         }
         // the collisions' tallies and voxel dose, aggregated over the warp
         if (__any_sync(FULL, scored && ntal > 0))
-            score_tallies_warp<R, MX>(scored && ntal > 0, MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, d0,
+            score_tallies_warp<R, MX, SPEC>(scored && ntal > 0, MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, d0,
                                       s, E0, cls0, scatter_class(n_coh, n_incoh), true, dep, words, scratch);
         {
             const DevJob& J = MULTI ? P.jobs[job] : P.job0;

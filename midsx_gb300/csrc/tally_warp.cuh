@@ -200,7 +200,9 @@ __device__ __forceinline__ void warp_record(int kind, unsigned long long* acc, i
 
 // score_tallies for the whole warp: lanes with `active` score the segment [p0, p0 + s d) of
 // their own job's tallies (same geometry and semantics as score_tallies), tally by tally.
-template <typename R, bool MX>
+// SPEC: also incident-energy spectra (per lane: a collision segment crosses a spectrum
+// surface rarely), compiled only into the kernels of launches that keep spectra.
+template <typename R, bool MX, bool SPEC = false>
 __device__ __forceinline__ void score_tallies_warp(bool active, const DevTally* tallies, int n_tallies,
                                                    const V3<R>& p0, const V3<R>& d, R s, R E, int cls0, int cls1,
                                                    bool interact, R dep, uint32_t& words,
@@ -304,8 +306,17 @@ __device__ __forceinline__ void score_tallies_warp(bool active, const DevTally* 
                     if (E != R(0)) ++words;
                     if (ec != R(0)) ++words;
                     ++words;
-                    // (no incident-energy spectra here: launches with spectrum tallies run
-                    // the lane-parking kernel)
+                    if constexpr (SPEC) {
+                        if (T.n_energy > 0) {
+                            const int kb = energy_bin<R>(T, E);
+                            if (kb >= 0) {
+                                unsigned long long* sp = T.acc + MIDSX_SCALAR_SLOTS + (size_t(kb) * 4 + cls0) * 2;
+                                count1(sp);
+                                Acc<MX>::cosine(sp + 1, ec);
+                                ++words;
+                            }
+                        }
+                    }
                 }
             }
         }

@@ -1329,16 +1329,16 @@ midsx_status launch_typed(midsx_tables_h tables, const RunParams& P, const midsx
     return MIDSX_OK;
 }
 
-template <typename R, bool MULTI, int TRACK>
+template <typename R, bool MULTI, int TRACK, bool SPEC>
 midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_run_config& cfg, int block,
                          cudaStream_t s) {
     const size_t smem = pool_smem<R>(P.n_jobs, MULTI, tables->T.n_materials, block);
     if (smem > 48 * 1024)
-        CUDA_TRY(cudaFuncSetAttribute(transport_pool_kernel<R, MULTI, TRACK>,
+        CUDA_TRY(cudaFuncSetAttribute(transport_pool_kernel<R, MULTI, TRACK, SPEC>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = cfg.blocks_per_sm;
     if (per_sm <= 0) {
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_pool_kernel<R, MULTI, TRACK>, block,
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_pool_kernel<R, MULTI, TRACK, SPEC>, block,
                                                                smem));
         per_sm = std::max(per_sm, 1);
     }
@@ -1349,7 +1349,7 @@ midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_
     // a warp keeps two photons per lane in flight
     uint64_t want = (P.total + 2 * uint64_t(block) - 1) / (2 * uint64_t(block));
     uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(tables->sm_count) * per_sm));
-    transport_pool_kernel<R, MULTI, TRACK><<<unsigned(grid), block, smem, s>>>(P);
+    transport_pool_kernel<R, MULTI, TRACK, SPEC><<<unsigned(grid), block, smem, s>>>(P);
     CUDA_TRY(cudaGetLastError());
     return MIDSX_OK;
 }
@@ -1357,13 +1357,27 @@ midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_
 template <typename R, bool MULTI>
 midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_run_config& cfg, int block,
                          cudaStream_t s) {
+    // spectra: single-job launches only (batched launches with spectra run the lane-parking
+    // kernel), so that their instantiations stay few
+    if constexpr (!MULTI) {
+        if (P.spectra) {
+            switch (P.tracking) {
+                case MIDSX_TRACK_BACKGROUND_FAST:
+                    return launch_pool<R, false, MIDSX_TRACK_BACKGROUND_FAST, true>(tables, P, cfg, block, s);
+                case MIDSX_TRACK_MACRO_CELL:
+                    return launch_pool<R, false, MIDSX_TRACK_MACRO_CELL, true>(tables, P, cfg, block, s);
+                default:
+                    return launch_pool<R, false, MIDSX_TRACK_REFERENCE, true>(tables, P, cfg, block, s);
+            }
+        }
+    }
     switch (P.tracking) {
         case MIDSX_TRACK_BACKGROUND_FAST:
-            return launch_pool<R, MULTI, MIDSX_TRACK_BACKGROUND_FAST>(tables, P, cfg, block, s);
+            return launch_pool<R, MULTI, MIDSX_TRACK_BACKGROUND_FAST, false>(tables, P, cfg, block, s);
         case MIDSX_TRACK_MACRO_CELL:
-            return launch_pool<R, MULTI, MIDSX_TRACK_MACRO_CELL>(tables, P, cfg, block, s);
+            return launch_pool<R, MULTI, MIDSX_TRACK_MACRO_CELL, false>(tables, P, cfg, block, s);
         default:
-            return launch_pool<R, MULTI, MIDSX_TRACK_REFERENCE>(tables, P, cfg, block, s);
+            return launch_pool<R, MULTI, MIDSX_TRACK_REFERENCE, false>(tables, P, cfg, block, s);
     }
 }
 
@@ -1379,11 +1393,13 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
         set_last_error("unknown tracking");
         return MIDSX_INVALID_ARG;
     }
-    if (P.spectra && (cfg.scheduler == MIDSX_SCHED_POOL || cfg.tracking != MIDSX_TRACK_REFERENCE)) {
-        set_last_error("incident-energy spectra are scored by the lane-parking scheduler with reference tracking");
+    // batched launches with spectra run the lane-parking kernel (reference tracking)
+    if (P.spectra && multi && (cfg.scheduler == MIDSX_SCHED_POOL || cfg.tracking != MIDSX_TRACK_REFERENCE)) {
+        set_last_error("batched launches with incident-energy spectra run the lane-parking scheduler with reference "
+                       "tracking");
         return MIDSX_INVALID_ARG;
     }
-    const bool pool = cfg.scheduler != MIDSX_SCHED_LANES && P.trace == nullptr && !P.spectra &&
+    const bool pool = cfg.scheduler != MIDSX_SCHED_LANES && P.trace == nullptr && !(P.spectra && multi) &&
                       (cfg.scheduler == MIDSX_SCHED_POOL || kDefaultScheduler == MIDSX_SCHED_POOL);
     if (cfg.tracking != MIDSX_TRACK_REFERENCE && !pool) {
         set_last_error("background fast and macro-cell tracking run in the photon-pool scheduler only");

@@ -233,6 +233,31 @@ def test_gpu_polyenergetic_hvl_through_spectrum_air_kerma(golden, case, precisio
 
 
 @pytest.mark.gpu
+def test_gpu_hvl_air_kerma_with_background_fast_tracking(golden):
+    """The half-value-layer scene is a thin slab in 100 cm of air: background fast tracking
+    takes the air gap in a few flights instead of a few hundred Woodcock steps, and the
+    spectrum air kerma agrees with the reference tracking."""
+    tables = M.Tables([scenes.AIR, scenes.ALUMINIUM], e_max=150e3)
+    src_d = hvl_source(golden, "30kVp")
+    tally = hvl_tally(golden, src_d)
+    sc = golden["scene"]
+    ids, spacing = hvl_geometry(golden, "30kVp", "hvl")
+    ph = M.Phantom(tables, sc["domain"], spacing, sc["slab_origin"], ids, scenes.AIR)
+    n = 1_000_000
+    ak, prim, steps = {}, {}, {}
+    for tracking, seed in (("reference", 51), ("background_fast", 52)):
+        tl = M.Tallies(ph, [tally], N.DOSE_OFF)
+        M.run(tables, ph, M.Source(**src_d), tl, n, seed=seed, precision="mixed", tracking=tracking)
+        ak[tracking] = D.primary_spectrum_air_kerma(tl, 0, tables, MIDPOINTS)
+        prim[tracking] = tl.spectrum(0)[0][:, 0].sum()
+        steps[tracking] = tl.stats()["steps"] / n
+    assert steps["background_fast"] * 20 < steps["reference"], steps
+    p = prim["reference"] / n
+    sig = ak["reference"] * np.sqrt(2 * (1 - p) / (n * p))
+    assert abs(ak["background_fast"] - ak["reference"]) < 4 * sig, (ak, sig)
+
+
+@pytest.mark.gpu
 def test_gpu_spectrum_mixed_matches_fp64_and_validation():
     """Mixed and FP64 forms on identical streams give the same primary spectrum (primary
     energies are exact source lines in both), and invalid spectrum specs are refused."""
@@ -262,10 +287,20 @@ def test_gpu_spectrum_mixed_matches_fp64_and_validation():
     tl = M.Tallies(ph, [dict(spec, spectrum=None)], N.DOSE_OFF)
     with pytest.raises(N.MidsxError):
         N.check(N.load().midsx_gpu_fetch_spectrum(tl.handle, 0, None, None, None), "fetch")
-    # spectra are scored by the lane-parking scheduler with reference tracking
-    tl = M.Tallies(ph, [spec], N.DOSE_OFF)
-    for kw in (dict(scheduler="pool"), dict(tracking="background_fast"), dict(tracking="macro_cell")):
-        with pytest.raises(N.MidsxError) as e:
-            M.run(tables, ph, src, tl, 100, seed=1, **kw)
-        assert e.value.status == N.INVALID_ARG, kw
-    M.run(tables, ph, src, tl, 100, seed=1, scheduler="lanes")
+    # single runs score spectra with either scheduler (same trajectories: identical integer
+    # words in the mixed form) and any tracking
+    got = {}
+    for sched in ("pool", "lanes"):
+        tl = M.Tallies(ph, [spec], N.DOSE_OFF)
+        M.run(tables, ph, src, tl, 50_000, seed=4, precision="mixed", scheduler=sched)
+        got[sched] = tl.spectrum(0)
+    np.testing.assert_array_equal(got["pool"][0], got["lanes"][0])
+    np.testing.assert_array_equal(got["pool"][1], got["lanes"][1])
+    for tracking in ("background_fast", "macro_cell"):
+        tl = M.Tallies(ph, [spec], N.DOSE_OFF)
+        M.run(tables, ph, src, tl, 1000, seed=1, tracking=tracking)
+        assert tl.spectrum(0)[0].sum() > 0
+    with pytest.raises(N.MidsxError) as e:
+        M.run(tables, ph, src, M.Tallies(ph, [spec], N.DOSE_OFF), 100, seed=1, scheduler="lanes",
+              tracking="background_fast")
+    assert e.value.status == N.INVALID_ARG
