@@ -245,6 +245,7 @@ def main():
               "config": {"workload": sc.name, "histories_per_step": N_hist, "precision": "mixed",
                          "voxels": ph.n_voxels, "dose_tally": "count/sum/sumsq per voxel (268 MB)",
                          "l2": "flushed between steps (256 MB write) and tally > L2",
+                         "launch": "photon pool, 128-thread blocks, 2 Woodcock steps per pass (defaults)",
                          "parallelism": "replicas over history ranges" if world > 1 else "single GPU"},
               "clocks": clk, "gpu_launches": args.steps,
               "step_latency_ms": {"p50": statistics.median(step_ms), "p99": float(np.percentile(step_ms, 99))},

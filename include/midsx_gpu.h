@@ -333,7 +333,11 @@ typedef struct midsx_run_config {
                                     (0 = 1) */
     int32_t scheduler;           /* midsx_scheduler */
     int32_t tracking;            /* midsx_tracking */
-    int32_t reserved;
+    int32_t steps_per_pass;      /* batched photon-pool launches: Woodcock steps a lane takes
+                                    between the warp's list bookkeeping, 1..4 (0 = tuned
+                                    default: 2 for the FP32 form with reference tracking, else
+                                    1; the request server's default is 1).  Single runs use
+                                    the default, fixed at compile time. */
     uint64_t seed;
     uint64_t first_history;      /* history ids [first, first + n) select Philox streams */
     uint64_t n_histories;

@@ -20,12 +20,13 @@
 
 constexpr int kPoolSlots = 64;        // photon slots per warp
 // Woodcock steps a lane takes per pass of the warp loop before the pool's bookkeeping
-// (ready and event lists, ballots) runs.  FP32 reference tracking: 2 against 1 measured +5.5
-// to +10 % on the cone-beam dose workload (3, 4 and 6 were slower than 1).  The FP64 form
-// (-2.3 % with 2) and the opt-in modes, whose steps are long (a background flight, a cell
-// walk; -8 to -9 % with 2), keep one.  A photon that parks ends its pass early.
+// (ready and event lists, ballots) runs.  Single-job kernels fix it at compile time (a
+// run-time bound cost the cone-beam dose workload 1 %): 2 for the FP32 form with reference
+// tracking, else 1 (default_steps_per_pass in transport.cu gives the measurements); batched
+// kernels take RunParams::steps_per_pass (the request server's mixed launches want 1, the
+// 64-job batch 2, the autotuner tries both).  A photon that parks ends its pass early.
 template <typename R, int TRACK>
-__host__ __device__ constexpr int steps_per_pass() {
+__host__ __device__ constexpr int single_job_steps_per_pass() {
     return TRACK == MIDSX_TRACK_REFERENCE && sizeof(R) == 4 ? 2 : 1;
 }
 constexpr uint32_t kKindFlight = 0u;  // slot kinds (meta bits 30-31)
@@ -239,7 +240,8 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         }
         if (__ballot_sync(FULL, cur >= 0) == 0u && rdy_top == 0 && ev_top == 0) break;
         uint32_t park = kKindFlight;
-        for (int pass = 0; pass < steps_per_pass<R, TRACK>() && park == kKindFlight && cur >= 0; ++pass) {
+        const int npass = MULTI ? P.steps_per_pass : single_job_steps_per_pass<R, TRACK>();
+        for (int pass = 0; pass < npass && park == kKindFlight && cur >= 0; ++pass) {
             bool segment = false;  // the step's segment goes to the tallies (escape or delta step)
             if (cur >= 0) {
                 // one Woodcock step: getFreePath, move, domain test, voxel fetch, isDeltaScatter

@@ -122,8 +122,19 @@ struct RunParams {
     int regroup;    // lanes of a warp that wait for an event before the warp runs the events
     int chunk;      // histories a lane reserves per fetch
     double* trace;  // optional (single job): energy deposited in grid voxels per history
-    int spectra;    // some tally of the launch keeps an incident-energy spectrum (lane-parking kernel)
+    int spectra;    // some tally of the launch keeps an incident-energy spectrum
+    int steps_per_pass;  // photon pool: Woodcock steps per pass of the warp loop
+    int server;          // launched by the request server (its own steps_per_pass default)
 };
+
+// Default Woodcock steps per pass of the photon-pool loop.  FP32 reference tracking: 2
+// against 1 measured +5.5 to +10 % on the cone-beam dose workload and +6 % on the 64-job
+// batch (3, 4 and 6 were slower than 1).  The FP64 form (-2.3 % with 2), the opt-in modes
+// whose steps are long (a background flight, a cell walk; -8 to -9 % with 2) and the request
+// server's short mixed launches (-10 % histories/s, +12 % p99 latency with 2) keep one.
+inline int default_steps_per_pass(int precision, int tracking, bool server) {
+    return precision == MIDSX_PREC_MIXED && tracking == MIDSX_TRACK_REFERENCE && !server ? 2 : 1;
+}
 
 // -------------------------------------------------------------------- atomics ---
 template <bool MX>
@@ -1406,6 +1417,12 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
         return MIDSX_INVALID_ARG;
     }
     P.tracking = cfg.tracking;
+    if (cfg.steps_per_pass < 0 || cfg.steps_per_pass > 4) {
+        set_last_error("steps_per_pass is 0 (default) or 1..4");
+        return MIDSX_INVALID_ARG;
+    }
+    P.steps_per_pass = cfg.steps_per_pass > 0 ? cfg.steps_per_pass
+                                               : default_steps_per_pass(cfg.precision, cfg.tracking, P.server != 0);
     P.max_steps = cfg.max_steps > 0 ? cfg.max_steps : 100000;
     P.max_trials = cfg.max_compton_trials > 0 ? cfg.max_compton_trials : 100000;
     P.regroup = cfg.regroup > 0 ? std::min(cfg.regroup, 32) : (pool ? 32 : 24);
@@ -2020,14 +2037,15 @@ extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precis
         bool spectra = false;
         for (auto* t : b->tallies) spectra |= t->spectra;
         if (!spectra)
-        for (int bs : {64, 128, 256})
-            for (int ps : {0})
-                for (int rg : {24, 28, 32}) {
-                    c.block_size = bs;
-                    c.blocks_per_sm = ps;
-                    c.regroup = rg;
-                    cands.push_back(c);
-                }
+            for (int bs : {64, 128, 256})
+                for (int sp : {1, 2})
+                    for (int rg : {24, 28, 32}) {
+                        c.block_size = bs;
+                        c.blocks_per_sm = 0;
+                        c.steps_per_pass = sp;
+                        c.regroup = rg;
+                        cands.push_back(c);
+                    }
     }
     double best_r = -1;
     RunParams P;
@@ -2146,6 +2164,7 @@ midsx_status launch_packed(midsx_tables_h tables, const void* dev_jobs, int n_jo
     P.counter = dev_counter;
     P.total = total;
     P.spectra = spectra;
+    P.server = 1;
     return launch_kernel(tables, P, cfg, true, s);
 }
 
