@@ -558,6 +558,23 @@ bool cuda_ok(cudaError_t e, const char* what) {
     return false;
 }
 
+// Runs `f` when the scope ends unless release() was called: the early error returns of a
+// create function free what it has allocated so far, and scratch buffers are freed on every
+// return.
+template <typename F>
+struct ScopeExit {
+    F f;
+    bool armed = true;
+    ~ScopeExit() {
+        if (armed) f();
+    }
+    void release() { armed = false; }
+};
+template <typename F>
+ScopeExit<F> scope_exit(F f) {
+    return ScopeExit<F>{f};
+}
+
 #define CUDA_TRY(call)                                          \
     do {                                                        \
         if (!cuda_ok((call), #call)) return MIDSX_CUDA_ERROR;   \
@@ -682,18 +699,14 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
     }
     auto* h = new midsx_gpu_tables();
     std::memset(&h->T, 0, sizeof(h->T));
+    auto guard = scope_exit([h] { midsx_gpu_tables_destroy(h); });
     CUDA_TRY(cudaGetDevice(&h->device));
     CUDA_TRY(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device));
     size_t nd = size_t(blob->n_data), ni = size_t(blob->n_idata);
     if (!cuda_ok(cudaMalloc(&h->d, nd * sizeof(double)), "cudaMalloc") ||
         !cuda_ok(cudaMalloc(&h->f, nd * sizeof(float)), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&h->rows, ni * sizeof(int)), "cudaMalloc")) {
-        cudaFree(h->d);
-        cudaFree(h->f);
-        cudaFree(h->rows);
-        delete h;
+        !cuda_ok(cudaMalloc(&h->rows, ni * sizeof(int)), "cudaMalloc"))
         return MIDSX_OOM;
-    }
     std::vector<int> rows(ni);
     for (size_t i = 0; i < ni; ++i) rows[i] = int(blob->idata[i]);
     CUDA_TRY(cudaMemcpy(h->d, blob->data, nd * sizeof(double), cudaMemcpyHostToDevice));
@@ -741,12 +754,10 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
     }
     for (int k = 0; k < 2; ++k)
         for (int p = 0; p < 2; ++p) T.bs[k][p] = bb.spec[k][p];
-    if (!cuda_ok(cudaMalloc(&h->bk, bb.data.size() * sizeof(int)), "cudaMalloc")) {
-        midsx_gpu_tables_destroy(h);
-        return MIDSX_OOM;
-    }
+    if (!cuda_ok(cudaMalloc(&h->bk, bb.data.size() * sizeof(int)), "cudaMalloc")) return MIDSX_OOM;
     CUDA_TRY(cudaMemcpy(h->bk, bb.data.data(), bb.data.size() * sizeof(int), cudaMemcpyHostToDevice));
     T.bk = h->bk;
+    guard.release();
     *out = h;
     return MIDSX_OK;
 }
@@ -1017,6 +1028,7 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
         return MIDSX_INVALID_ARG;
     }
     auto* s = new midsx_gpu_source();
+    auto guard = scope_exit([s] { midsx_gpu_source_destroy(s); });
     DevSource& S = s->S;
     std::memset(&S, 0, sizeof(S));
     for (int i = 0; i < 3; ++i) {
@@ -1032,7 +1044,6 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
     if (spec->direction_kind == MIDSX_DIR_RECTANGLE) {
         double d = spec->b[0] * spec->c[0] + spec->b[1] * spec->c[1] + spec->b[2] * spec->c[2];
         if (std::fabs(d) >= 1e-9) {
-            delete s;
             set_last_error("Edges are not orthogonal");
             return MIDSX_INVALID_ARG;
         }
@@ -1067,7 +1078,6 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
     if (spec->spectrum_kind == MIDSX_SPEC_POLY) {
         int nb = spec->n_bins;
         if (nb < 1 || nb > MIDSX_MAX_SPECTRUM_BINS || !spec->bin_energy || !spec->bin_prob) {
-            delete s;
             set_last_error("bad spectrum");
             return MIDSX_INVALID_ARG;
         }
@@ -1115,7 +1125,6 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
         S.f_guide = gbuf + kCdfGuide + 1;
     } else {
         if (!(spec->mono_energy > 0)) {
-            delete s;
             set_last_error("bad mono energy");
             return MIDSX_INVALID_ARG;
         }
@@ -1129,6 +1138,7 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
     }
     S.f_radius = float(S.radius);
     S.f_mono = float(S.mono);
+    guard.release();
     *out = s;
     return MIDSX_OK;
 }
@@ -1237,27 +1247,24 @@ extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const 
         return MIDSX_INVALID_ARG;
     }
     auto* t = new midsx_gpu_tallies();
+    auto guard = scope_exit([t] { midsx_gpu_tallies_destroy(t); });
     midsx_status lst = tallies_layout(phantom ? phantom->n_voxels : 0, specs, n_specs, dose_mode, t);
-    if (lst != MIDSX_OK) {
-        delete t;
-        return lst;
-    }
+    if (lst != MIDSX_OK) return lst;
     const size_t words = t->acc_words;
     // run statistics plus one word: the launch's history counter
     if (!cuda_ok(cudaMalloc(&t->stats, (kStCount + 1) * sizeof(unsigned long long)), "cudaMalloc") ||
         (words && !cuda_ok(cudaMalloc(&t->acc, words * 8), "cudaMalloc")) ||
         (n_specs && !cuda_ok(cudaMalloc(&t->specs, n_specs * sizeof(DevTally)), "cudaMalloc")) ||
         (t->dose_stride &&
-         !cuda_ok(cudaMalloc(&t->dose, t->n_voxels * t->dose_stride * sizeof(unsigned long long)), "cudaMalloc"))) {
-        midsx_gpu_tallies_destroy(t);
+         !cuda_ok(cudaMalloc(&t->dose, t->n_voxels * t->dose_stride * sizeof(unsigned long long)), "cudaMalloc")))
         return MIDSX_OOM;
-    }
     for (auto& d : t->host_specs) d.acc = t->acc + reinterpret_cast<size_t>(d.acc);
     if (n_specs)
         CUDA_TRY(cudaMemcpy(t->specs, t->host_specs.data(), n_specs * sizeof(DevTally), cudaMemcpyHostToDevice));
     midsx_status st = midsx_gpu_tallies_reset(t, nullptr);
     if (st != MIDSX_OK) return st;
     CUDA_TRY(cudaDeviceSynchronize());
+    guard.release();
     *out = t;
     return MIDSX_OK;
 }
@@ -1794,6 +1801,10 @@ extern "C" midsx_status midsx_gpu_sample(midsx_tables_h tables, int32_t precisio
         return MIDSX_INVALID_ARG;
     if (kind == 0 && energy > tables->T.e_max) return MIDSX_TABLE_RANGE;
     double *d0 = nullptr, *d1 = nullptr;
+    auto guard = scope_exit([&] {
+        cudaFree(d0);
+        cudaFree(d1);
+    });
     CUDA_TRY(cudaMalloc(&d0, n * sizeof(double)));
     CUDA_TRY(cudaMalloc(&d1, n * sizeof(double)));
     unsigned grid = unsigned((n + 255) / 256);
@@ -1804,8 +1815,6 @@ extern "C" midsx_status midsx_gpu_sample(midsx_tables_h tables, int32_t precisio
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpy(out0, d0, n * sizeof(double), cudaMemcpyDeviceToHost));
     if (out1) CUDA_TRY(cudaMemcpy(out1, d1, n * sizeof(double), cudaMemcpyDeviceToHost));
-    cudaFree(d0);
-    cudaFree(d1);
     return MIDSX_OK;
 }
 
@@ -1815,14 +1824,16 @@ extern "C" midsx_status midsx_gpu_table_index(midsx_tables_h tables, int32_t mat
         return MIDSX_INVALID_ARG;
     double* de = nullptr;
     int64_t* di = nullptr;
+    auto guard = scope_exit([&] {
+        cudaFree(de);
+        cudaFree(di);
+    });
     CUDA_TRY(cudaMalloc(&de, n * sizeof(double)));
     CUDA_TRY(cudaMalloc(&di, 6 * n * sizeof(int64_t)));
     CUDA_TRY(cudaMemcpy(de, e, n * sizeof(double), cudaMemcpyHostToDevice));
     index_kernel<<<unsigned((n + 255) / 256), 256>>>(tables->T, material, de, n, di);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpy(idx, di, 6 * n * sizeof(int64_t), cudaMemcpyDeviceToHost));
-    cudaFree(de);
-    cudaFree(di);
     return MIDSX_OK;
 }
 
@@ -1894,22 +1905,17 @@ extern "C" midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const mids
         return MIDSX_INVALID_ARG;
     }
     auto* b = new midsx_gpu_batch();
+    auto guard = scope_exit([b] { midsx_gpu_batch_destroy(b); });
     b->tables = tables;
     b->n_jobs = n_jobs;
     b->host_prefix.push_back(0);
     for (int i = 0; i < n_jobs; ++i) {
         const midsx_batch_job& j = jobs[i];
         midsx_status cst = check_job(tables, j.phantom, j.source, j.tallies, "batch job " + std::to_string(i));
-        if (cst != MIDSX_OK) {
-            delete b;
-            return cst;
-        }
+        if (cst != MIDSX_OK) return cst;
         // the tracking of the batch's launches is not known yet: the cells exist for any
         cst = ensure_cells(j.phantom);
-        if (cst != MIDSX_OK) {
-            delete b;
-            return cst;
-        }
+        if (cst != MIDSX_OK) return cst;
         DevJob d;
         std::memset(&d, 0, sizeof(d));
         fill_job(d, j.phantom, j.source, j.tallies, j.seed, j.first_history, j.n_histories);
@@ -1920,14 +1926,13 @@ extern "C" midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const mids
     }
     if (!cuda_ok(cudaMalloc(&b->jobs, n_jobs * sizeof(DevJob)), "cudaMalloc") ||
         !cuda_ok(cudaMalloc(&b->prefix, (n_jobs + 1) * sizeof(unsigned long long)), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&b->words, 2 * sizeof(unsigned long long)), "cudaMalloc")) {
-        midsx_gpu_batch_destroy(b);
+        !cuda_ok(cudaMalloc(&b->words, 2 * sizeof(unsigned long long)), "cudaMalloc"))
         return MIDSX_OOM;
-    }
     CUDA_TRY(cudaMemcpy(b->jobs, b->host_jobs.data(), n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(b->prefix, b->host_prefix.data(), (n_jobs + 1) * sizeof(unsigned long long),
                         cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemset(b->words, 0, 2 * sizeof(unsigned long long)));
+    guard.release();
     *out = b;
     return MIDSX_OK;
 }
@@ -2009,9 +2014,14 @@ extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precis
         tp.push_back(tp.back() + k);
     }
     unsigned long long* dprefix = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto guard = scope_exit([&] {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaFree(dprefix);
+    });
     CUDA_TRY(cudaMalloc(&dprefix, tp.size() * sizeof(unsigned long long)));
     CUDA_TRY(cudaMemcpy(dprefix, tp.data(), tp.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice));
-    cudaEvent_t e0, e1;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
     // candidate launch shapes: both schedulers, their block sizes, occupancy and regroup
@@ -2074,9 +2084,6 @@ extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precis
             }
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(dprefix);
     if (st != MIDSX_OK) return st;
     for (auto* t : b->tallies) {
         st = midsx_gpu_tallies_reset(t, stream);
