@@ -320,15 +320,26 @@ def main():
     if os.path.exists(peaks_path):
         peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
     traffic = None
+    profile = {}
     tpath = os.path.join(ROOT, "profiles", "transport_traffic.txt")
     if os.path.exists(tpath):
         for line in open(tpath):
-            if line.startswith("dram_bytes_per_history"):
-                traffic = float(line.split()[1]) * N_hist
+            if line and not line.startswith("#") and len(line.split()) == 2:
+                profile[line.split()[0]] = float(line.split()[1])
+    if "dram_bytes_per_history" in profile:
+        traffic = profile["dram_bytes_per_history"] * N_hist
     result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                           "bytes_per_history": b_hist, "F": F, "W": W,
                           "kernel_ms": 1e3 * kernel_s}
+    if "issue_active_pct" in profile:
+        # neither HBM nor a tensor pipe limits this kernel: dependent-latency chains per warp
+        result["roofline"]["limiter"] = {
+            "kind": "latency (dependent chains per warp), not bandwidth",
+            "issue_active_pct": profile["issue_active_pct"],
+            "warps_active_per_sm": profile.get("warps_active_per_sm"),
+            "lanes_per_instruction": profile.get("lanes_per_instruction"),
+            "source": "ncu capture of 1e6 histories (profiles/transport_traffic.txt)"}
     if "e2e" not in result:
         result["e2e"] = None
     if not args.quick:
