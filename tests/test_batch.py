@@ -52,6 +52,38 @@ def test_batch_jobs_equal_single_runs(setup):
         assert a[3]["histories"] == sc.n_histories
 
 
+@pytest.mark.parametrize("scheduler", ["lanes", "pool"])
+def test_batch_with_empty_jobs(setup, scheduler):
+    """Jobs of no histories, first, between and after the others, take no history ids: the
+    other jobs equal their single runs, the empty jobs' tallies stay zero, and a batch of
+    empty jobs only runs nothing."""
+    tables, jobs = setup
+    plan = [(jobs[0], 0), (jobs[0], jobs[0].n_histories), (jobs[1], 0), (jobs[1], jobs[1].n_histories),
+            (jobs[1], 0)]
+    objs = [make(tables, sc) for sc, _ in plan]
+    batch = M.Batch(tables, [(ph, src, tl, 40 + j, 0, n)
+                             for j, ((sc, n), (ph, src, tl)) in enumerate(zip(plan, objs))])
+    batch.run("mixed", scheduler=scheduler)
+    for j, (sc, n) in enumerate(plan):
+        a = results(objs[j][2])
+        assert a[3]["histories"] == n
+        if n == 0:
+            assert a[3]["steps"] == 0 and not any(np.any(x) for x in a[:3])
+            continue
+        ph, src, tl = make(tables, sc)
+        M.run(tables, ph, src, tl, n, seed=40 + j, precision="mixed", scheduler=scheduler)
+        b = results(tl)
+        for x, y in zip(a[:3], b[:3]):
+            np.testing.assert_array_equal(x, y)
+        assert a[3]["steps"] == b[3]["steps"]
+    empty = [make(tables, jobs[2]) for _ in range(2)]
+    nothing = M.Batch(tables, [(ph, src, tl, 1, 0, 0) for ph, src, tl in empty])
+    nothing.run("mixed", scheduler=scheduler)
+    for _, _, tl in empty:
+        st = tl.stats()
+        assert st["histories"] == 0 and st["steps"] == 0
+
+
 def test_batch_fp64_equals_single_runs(setup):
     tables, jobs = setup
     objs = [make(tables, sc) for sc in jobs[:2]]

@@ -76,6 +76,19 @@ def test_pool_few_histories(scene, n):
     same(run(scene, n, "mixed", "lanes", seed=9), run(scene, n, "mixed", "pool", seed=9), exact=True)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_zero_histories_leave_the_tallies_empty(scene, precision):
+    """A run of no histories launches nothing: statistics, dose, detector and scalar tallies
+    stay zero under both schedulers."""
+    for scheduler in ("lanes", "pool"):
+        out = run(scene, 0, precision, scheduler)
+        assert all(out["stats"][k] == 0 for k in EXACT_STATS)
+        for k in ("sum", "sumsq", "count"):
+            assert not np.any(out["dose"][k]), k
+        for arr in list(out["binned"]) + [out["disc"], out["cuboid"]]:
+            assert not np.any(np.asarray(arr, dtype=float))
+
+
 def test_pool_batched_equals_lanes():
     jobs = scenes.batch_jobs(n_jobs=5, seed=4, edge_range=(12, 40), hist_range=(3e3, 4e4), spacing=0.2)
     tables = M.Tables(jobs[0].materials, e_max=150e3)
