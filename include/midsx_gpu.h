@@ -49,7 +49,11 @@ typedef enum midsx_precision {
     MIDSX_PREC_MIXED = 1   /* FP32 transport, 64-bit fixed-point integer tallies */
 } midsx_precision;
 
-#define MIDSX_MAX_MATERIALS 16
+/* Materials of one table set: the TG-195 Case 5 voxel volume of the reference's CT example
+ * (cpp_simulations/CT_w_voxelized_solid) holds 20.  32 is also the width of a macro cell's
+ * material mask.  The photon caches in shared memory grow with the count: launches whose
+ * default block would not fit take a smaller one. */
+#define MIDSX_MAX_MATERIALS 32
 #define MIDSX_MAX_SPECTRUM_BINS 1024
 #define MIDSX_MAX_TALLIES 64
 

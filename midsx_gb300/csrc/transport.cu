@@ -515,6 +515,7 @@ struct midsx_gpu_tables {
     int32_t ids[MIDSX_MAX_MATERIALS];
     int device = 0;
     int sm_count = 0;
+    size_t max_smem = 0;  // opt-in shared memory of one block
 };
 
 struct midsx_gpu_phantom {
@@ -702,6 +703,9 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
     auto guard = scope_exit([h] { midsx_gpu_tables_destroy(h); });
     CUDA_TRY(cudaGetDevice(&h->device));
     CUDA_TRY(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device));
+    int optin = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+    h->max_smem = size_t(optin);
     size_t nd = size_t(blob->n_data), ni = size_t(blob->n_idata);
     if (!cuda_ok(cudaMalloc(&h->d, nd * sizeof(double)), "cudaMalloc") ||
         !cuda_ok(cudaMalloc(&h->f, nd * sizeof(float)), "cudaMalloc") ||
@@ -1399,6 +1403,14 @@ midsx_status launch_pool(midsx_tables_h tables, const RunParams& P, const midsx_
     }
 }
 
+// Shared-memory bytes of a launch of either scheduler.
+size_t launch_smem(int n_jobs, bool multi, bool mixed, bool pool, int n_materials, int block) {
+    if (pool) return mixed ? pool_smem<float>(n_jobs, multi, n_materials, block)
+                           : pool_smem<double>(n_jobs, multi, n_materials, block);
+    return mixed ? kernel_smem<float>(n_jobs, multi, n_materials, block)
+                 : kernel_smem<double>(n_jobs, multi, n_materials, block);
+}
+
 // Completes the launch parameters from cfg, zeroes the history counter and launches.  The
 // per-history trace is written by the lane-parking kernel only.
 midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_config& cfg, bool multi,
@@ -1440,6 +1452,16 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
     if (block > max_block || block % 32) {
         set_last_error(max_block == 128 ? "block_size must be a multiple of 32 up to 128 (photon pool, one job)"
                                         : "block_size must be a multiple of 32 up to 256");
+        return MIDSX_INVALID_ARG;
+    }
+    // the per-photon caches hold every material: with many materials the default block
+    // shrinks until its shared memory fits
+    const int M = tables->T.n_materials;
+    if (cfg.block_size <= 0)
+        while (block > 32 && launch_smem(P.n_jobs, multi, mixed, pool, M, block) > tables->max_smem) block /= 2;
+    if (launch_smem(P.n_jobs, multi, mixed, pool, M, block) > tables->max_smem) {
+        set_last_error("the shared memory of a " + std::to_string(block) + "-thread block (caches of " +
+                       std::to_string(M) + " materials) exceeds the device's: use a smaller block_size");
         return MIDSX_INVALID_ARG;
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -2064,6 +2086,9 @@ extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precis
         int last_sched = -1, last_block = -1;
         for (const midsx_run_config& cand : cands) {
             if (st != MIDSX_OK) break;
+            if (launch_smem(P.n_jobs, true, precision == MIDSX_PREC_MIXED, cand.scheduler == MIDSX_SCHED_POOL,
+                            b->tables->T.n_materials, cand.block_size) > b->tables->max_smem)
+                continue;  // too many materials for this block size
             // one warm-up launch per scheduler and block size is enough
             if (pass == 0 && cand.scheduler == last_sched && cand.block_size == last_block) continue;
             last_sched = cand.scheduler;

@@ -10,7 +10,7 @@ import numpy as np
 
 from . import build as _build
 
-MAX_MATERIALS = 16
+MAX_MATERIALS = 32
 SCALAR_SLOTS = 40
 MAX_ENERGY_BINS = 65536
 
