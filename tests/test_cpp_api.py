@@ -89,6 +89,22 @@ def test_scene_json_and_nifti_load_through_cpp_api(tmp_path):
         assert mus[mid] == pytest.approx(blob.eval(i, "total", np.array([60e3]))[0], rel=1e-12)
 
 
+def test_twenty_material_scene_loads_through_cpp_api(tmp_path):
+    """A grid of the twenty TG-195 Case 5 materials (ids 150-169) with "Air - C5" as the
+    background, as the reference's CT example sets it up: every material gets its tables."""
+    case5 = list(range(150, 170))
+    ids = np.array(case5, np.uint8).reshape(2, 2, 5)
+    js = write_scene(tmp_path, ids, (10.0, 10.0, 10.0), (1, 1, 1), (8, 8, 8), background="Air - C5")
+    r = subprocess.run([exe("scene_info"), js, "56400"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    d = parse(r.stdout)
+    assert sorted(int(m[0]) for m in d["material"]) == case5
+    blob = M.TableBlob(case5, e_max=150e3)
+    mus = {int(m[0]): float(m[-3]) for m in d["mu"]}
+    for i, mid in enumerate(case5):
+        assert mus[mid] == pytest.approx(blob.eval(i, "total", np.array([56.4e3]))[0], rel=1e-12)
+
+
 def test_gz_scene_loads_when_zlib_present(tmp_path):
     if not build._have_zlib():
         pytest.skip("built without zlib")
