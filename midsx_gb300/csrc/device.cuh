@@ -74,6 +74,41 @@ MIDSX_HD Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c
     return o;
 }
 
+// The same generator with the key schedule precomputed: rk[2r], rk[2r + 1] are round r's
+// keys (philox_round_keys).  A launch of one seed passes them as kernel parameters, so the
+// rounds read them from the constant bank instead of adding the Weyl increments per block.
+MIDSX_HD void philox_round_keys(uint64_t seed, uint32_t* rk) {
+    uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        rk[2 * r] = k0;
+        rk[2 * r + 1] = k1;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+MIDSX_HD Philox4 philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const uint32_t (&rk)[20]) {
+    uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0, lo0, hi1, lo1;
+        mulhilo32(0xD2511F53u, x0, hi0, lo0);
+        mulhilo32(0xCD9E8D57u, x2, hi1, lo1);
+        uint32_t y0 = hi1 ^ x1 ^ rk[2 * r];
+        uint32_t y2 = hi0 ^ x3 ^ rk[2 * r + 1];
+        x0 = y0;
+        x1 = lo1;
+        x2 = y2;
+        x3 = lo0;
+    }
+    Philox4 o;
+    o.v[0] = x0;
+    o.v[1] = x1;
+    o.v[2] = x2;
+    o.v[3] = x3;
+    return o;
+}
+
 // One random stream per history: draw n uses 64 bits of Philox block (n >> 1) with
 // counter (n >> 1, history_lo, history_hi, 0) and key (seed_lo, seed_hi).  The FP64 path
 // uses the top 53 bits, the FP32 path the top 24 bits of the same 64-bit word, so both
@@ -110,6 +145,16 @@ struct HistoryRng {
     MIDSX_HD void next_pair64(uint64_t& first, uint64_t& second) {
         uint32_t blk = (n + 1u) >> 1;
         Philox4 w = philox4x32_10(blk, h0, h1, 0u, k0, k1);
+        first = (uint64_t(w.v[0]) << 32) | w.v[1];
+        second = (uint64_t(w.v[2]) << 32) | w.v[3];
+        b0 = w.v[2];
+        b1 = w.v[3];
+        n = 2u * blk + 2u;
+    }
+    // next_pair64 with the stream's key schedule precomputed (philox_round_keys of its seed)
+    MIDSX_HD void next_pair64_rk(uint64_t& first, uint64_t& second, const uint32_t (&rk)[20]) {
+        uint32_t blk = (n + 1u) >> 1;
+        Philox4 w = philox4x32_10_rk(blk, h0, h1, 0u, rk);
         first = (uint64_t(w.v[0]) << 32) | w.v[1];
         second = (uint64_t(w.v[2]) << 32) | w.v[3];
         b0 = w.v[2];

@@ -253,7 +253,10 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
                 } else {
                     ++steps;
                     uint64_t w1, w2;
-                    rng.next_pair64(w1, w2);
+                    if constexpr (MULTI)
+                        rng.next_pair64(w1, w2);
+                    else
+                        rng.next_pair64_rk(w1, w2, P.round_keys);
                     // MIDSX_TRACK_BACKGROUND_FAST: a photon known to be in the background (vox == -1
                     // after its last voxel lookup) flies against the background's own attenuation,
                     // exact there, up to the first grid it would enter

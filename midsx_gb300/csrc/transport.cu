@@ -125,6 +125,7 @@ struct RunParams {
     int spectra;    // some tally of the launch keeps an incident-energy spectrum
     int steps_per_pass;  // photon pool: Woodcock steps per pass of the warp loop
     int server;          // launched by the request server (its own steps_per_pass default)
+    uint32_t round_keys[20];  // single-job launch: Philox key schedule of job0.seed
 };
 
 // Default Woodcock steps per pass of the photon-pool loop.  FP32 reference tracking: 2
@@ -1515,6 +1516,7 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
     std::memset(&P, 0, sizeof(P));
     P.T = tables->T;
     fill_job(P.job0, phantom, source, tallies, cfg->seed, cfg->first_history, cfg->n_histories);
+    philox_round_keys(cfg->seed, P.round_keys);
     P.n_jobs = 1;
     P.counter = tallies->stats + kStCount;
     P.total = cfg->n_histories;
