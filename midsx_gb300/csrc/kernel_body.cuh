@@ -112,34 +112,6 @@ __device__ __forceinline__ unsigned long long fx_stat(float e) {
     return (unsigned long long)__float2uint_rn(e * float(kFxStat));
 }
 
-// Geometry of one job in the working precision (ComputationalDomain with one voxel grid).
-template <typename R>
-struct Geo {
-    V3<R> dom, org, ext, spc, ispc;
-    int nx, ny, nz, bg;
-    const uint8_t* ids;
-    int n_grids;           // grids of the domain; the first is held above
-    const DevGrid* extra;  // the others, in first-hit order
-};
-
-template <typename R>
-__device__ Geo<R> make_geo(const DevGeom& G) {
-    Geo<R> g;
-    g.dom = {R(G.domain[0]), R(G.domain[1]), R(G.domain[2])};
-    g.org = {R(G.origin[0]), R(G.origin[1]), R(G.origin[2])};
-    g.ext = {R(G.ext[0]), R(G.ext[1]), R(G.ext[2])};
-    g.spc = {R(G.spacing[0]), R(G.spacing[1]), R(G.spacing[2])};
-    g.ispc = {R(1) / g.spc.x, R(1) / g.spc.y, R(1) / g.spc.z};
-    g.nx = G.dims[0];
-    g.ny = G.dims[1];
-    g.nz = G.dims[2];
-    g.bg = G.background;
-    g.ids = G.ids;
-    g.n_grids = G.n_grids;
-    g.extra = G.extra;
-    return g;
-}
-
 // Distance along the ray p + t d (t >= 0) to the closed box [lo, lo + ext], +inf if the ray
 // misses it (slab method) or meets it for no more than `tol` (grazing it, or leaving it from
 // a point within tol of its far side); 0 if p is inside.
@@ -469,7 +441,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
         for (int i = threadIdx.x; i < njobs; i += blockDim.x) s_geo[i] = make_geo<R>(P.jobs[i].G);
     }
     __syncthreads();
-    const Geo<R> g0 = make_geo<R>(P.job0.G);  // single-job launches
+    const Geo<R>& g0 = job0_geo(P, R(0));  // single-job launches
     const unsigned long long epoch = P.epoch ? *P.epoch : 0ull;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanes_below = (1u << lane) - 1u;

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
     S.meta[sbase + lane] = pack_meta(0, 0, 0, 0, kKindStart);
     S.meta[sbase + lane + 32] = pack_meta(0, 0, 0, 0, kKindStart);
     __syncthreads();
-    const Geo<R> g0 = make_geo<R>(P.job0.G);
+    const Geo<R>& g0 = job0_geo(P, R(0));
     const unsigned long long epoch = P.epoch ? *P.epoch : 0ull;
     const int regroup = max(1, min(P.regroup, 32));
     constexpr bool fast_mode = TRACK != MIDSX_TRACK_REFERENCE;   // background flights

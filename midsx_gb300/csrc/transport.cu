@@ -103,6 +103,34 @@ struct DevJob {
     uint64_t seed, first, n;
 };
 
+// Geometry of one job in the working precision (ComputationalDomain with one voxel grid).
+template <typename R>
+struct Geo {
+    V3<R> dom, org, ext, spc, ispc;
+    int nx, ny, nz, bg;
+    const uint8_t* ids;
+    int n_grids;           // grids of the domain; the first is held above
+    const DevGrid* extra;  // the others, in first-hit order
+};
+
+template <typename R>
+MIDSX_HD Geo<R> make_geo(const DevGeom& G) {
+    Geo<R> g;
+    g.dom = {R(G.domain[0]), R(G.domain[1]), R(G.domain[2])};
+    g.org = {R(G.origin[0]), R(G.origin[1]), R(G.origin[2])};
+    g.ext = {R(G.ext[0]), R(G.ext[1]), R(G.ext[2])};
+    g.spc = {R(G.spacing[0]), R(G.spacing[1]), R(G.spacing[2])};
+    g.ispc = {R(1) / g.spc.x, R(1) / g.spc.y, R(1) / g.spc.z};
+    g.nx = G.dims[0];
+    g.ny = G.dims[1];
+    g.nz = G.dims[2];
+    g.bg = G.background;
+    g.ids = G.ids;
+    g.n_grids = G.n_grids;
+    g.extra = G.extra;
+    return g;
+}
+
 constexpr int kMaxBatchJobs = 64;  // jobs of one batched launch (geometry staged in shared memory)
 // scheduler of MIDSX_SCHED_DEFAULT: the photon pool (cone-beam dose workload, 1e7 histories:
 // 2.65e8 histories/s against 2.27e8 for lane parking in FP32, 3.3e7 against 2.1e7 in FP64)
@@ -126,7 +154,12 @@ struct RunParams {
     int steps_per_pass;  // photon pool: Woodcock steps per pass of the warp loop
     int server;          // launched by the request server (its own steps_per_pass default)
     uint32_t round_keys[20];  // single-job launch: Philox key schedule of job0.seed
+    Geo<float> geo_f;         // single-job launch: job0's geometry in either precision,
+    Geo<double> geo_d;        // read by the kernels from the constant bank
 };
+
+__device__ __forceinline__ const Geo<float>& job0_geo(const RunParams& P, float) { return P.geo_f; }
+__device__ __forceinline__ const Geo<double>& job0_geo(const RunParams& P, double) { return P.geo_d; }
 
 // Default Woodcock steps per pass of the photon-pool loop.  FP32 reference tracking: 2
 // against 1 measured +5.5 to +10 % on the cone-beam dose workload and +6 % on the 64-job
@@ -1517,6 +1550,8 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
     P.T = tables->T;
     fill_job(P.job0, phantom, source, tallies, cfg->seed, cfg->first_history, cfg->n_histories);
     philox_round_keys(cfg->seed, P.round_keys);
+    P.geo_f = make_geo<float>(P.job0.G);
+    P.geo_d = make_geo<double>(P.job0.G);
     P.n_jobs = 1;
     P.counter = tallies->stats + kStCount;
     P.total = cfg->n_histories;
