@@ -36,7 +36,9 @@ public:
     void addVoxelDataToComputationalDomain();
 
     // GPU options (not in the reference): precision of the kernel, random seed and the
-    // first history id of the next run.
+    // first history id of the next run.  The default is the plain FP64 form, the drop-in for
+    // the reference's double-precision transport; MIDSX_PREC_MIXED (FP32 transport, 64-bit
+    // fixed-point tallies) is opt-in.
     void setPrecision(midsx_precision p) { precision_ = p; }
     void setSeed(uint64_t seed) { seed_ = seed; }
     // Opt-in flight sampling (midsx_tracking; the reference's global-majorant Woodcock
@@ -56,7 +58,7 @@ private:
     std::vector<std::unique_ptr<VolumeTally>> volume_tallies_;
     std::vector<std::unique_ptr<SurfaceTally>> surface_tallies_;
     std::unique_ptr<Device> dev_;
-    midsx_precision precision_ = MIDSX_PREC_MIXED;
+    midsx_precision precision_ = MIDSX_PREC_FP64;
     midsx_tracking tracking_ = MIDSX_TRACK_REFERENCE;
     int macro_edge_ = 0;  // 0: the phantom's own (MIDSX_MACRO_CELL)
     int macro_edge_applied_ = 0;

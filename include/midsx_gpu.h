@@ -327,7 +327,11 @@ typedef enum midsx_tracking {
 
 typedef struct midsx_run_config {
     int32_t precision;           /* midsx_precision */
-    int32_t max_steps;           /* per-history step cap (0 = 100000) */
+    int32_t max_steps;           /* per-history step cap (0 = derived per job: 16 crossings of the
+                                    domain diagonal at the largest majorant between min(1 keV,
+                                    the source's lowest energy) and the tables' e_max, at least
+                                    100000; hits are counted and make the fetches report
+                                    MIDSX_STEP_CAP) */
     int32_t max_compton_trials;  /* Kahn/S(x) rejection cap (0 = 100000) */
     int32_t block_size;          /* 0 = tuned default */
     int32_t blocks_per_sm;       /* 0 = tuned default */
@@ -549,13 +553,16 @@ midsx_status midsx_gpu_trace_deposits(midsx_tables_h tables, midsx_phantom_h pha
  * device-wide synchronisation cudaFree implies.  It calls no cudaMalloc, cudaFree or other
  * allocating routine: its scratch (run counters and one double per history) is a fixed array
  * in the library's device code, 8 MiB plus 256 bytes on every GPU that loads the library,
- * held until the process exits.  Limit: at most 1,048,576 histories per call; larger requests
- * fail with MIDSX_INVALID_ARG.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) and keeps it, so make that first call before any stream
- * capture.  All calls on a device share the one array, so calls whose device work overlaps
- * (different streams, different host threads) race on it; serialise them.  Inputs and the
- * host output hist_dep (n_histories doubles) are the caller's; the call returns when the
- * results are in hist_dep. */
+ * held until the process exits.  Limits: at most 1,048,576 histories per call, and reference
+ * tracking only (cfg->tracking = MIDSX_TRACK_REFERENCE: the other modes build macro cells,
+ * which allocate); other requests fail with MIDSX_INVALID_ARG before any device work.  Each
+ * call looks up the array's device address (cudaGetSymbolAddress) with the caller's device
+ * current; the first call on a device also loads the library's device code there, so make
+ * that first call before any stream capture.  All calls on a device share the one array,
+ * which keeps the last call's contents (the call clears its counters itself), so calls whose
+ * device work overlaps (different streams, different host threads) race on it; serialise
+ * them.  Inputs and the host output hist_dep (n_histories doubles) are the caller's.  The
+ * call is synchronous: it returns when the results are in hist_dep. */
 midsx_status midsx_gpu_trace_deposits_noalloc(midsx_tables_h tables, midsx_phantom_h phantom,
                                               midsx_source_h source, const midsx_run_config* cfg,
                                               double* hist_dep, void* stream);

@@ -291,7 +291,10 @@ class Tallies:
     def reset(self, stream=None):
         N.check(N.load().midsx_gpu_tallies_reset(self.handle, stream), "midsx_gpu_tallies_reset")
 
-    def stats(self, stream=None, allow_cap=True):
+    def stats(self, stream=None, allow_cap=False):
+        """Run statistics.  A history that reached the step or Compton-trial cap was cut short
+        (the reference's loop has no cap), so that raises MidsxError(STEP_CAP) unless the caller
+        opts in with allow_cap=True (e.g. a test that sets a tiny cap on purpose)."""
         st = N.RunStats()
         N.check(N.load().midsx_gpu_fetch_stats(self.handle, C.byref(st), stream), "midsx_gpu_fetch_stats",
                 allow=(N.STEP_CAP,) if allow_cap else ())

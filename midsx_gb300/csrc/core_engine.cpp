@@ -145,7 +145,9 @@ double PhysicsEngine::run(PhotonSource& source, uint64_t n_photons) {
     if (st == MIDSX_OK) st = midsx_gpu_fetch_stats(dev_->tallies, &stats_, nullptr);
     double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     midsx_gpu_source_destroy(src);
-    if (st == MIDSX_STEP_CAP) st = MIDSX_OK;  // counted in lastStats(); the histories are retired
+    // a history that reached the step or Compton-trial cap was cut short, which the reference's
+    // unbounded loop never does: the run's results would be biased, so it is an error (the
+    // counts stay in lastStats())
     check(st, "midsx_gpu_run");
     next_history_ += n_photons;
     // scalar and binned tallies: the device holds cumulative sums over all runs

@@ -21,18 +21,21 @@ size_t job_record_bytes();
 // Validates one job (handles made with `tables`, dose tally sized for the phantom, source
 // energy inside the tables and, for the mixed form, under its fixed-point limit; tallies
 // empty or of the same precision) and writes its device record into host memory `dst`.
+// step_cap (optional) receives the job's default per-history step cap (derived from its
+// domain, source and tables).
 midsx_status pack_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_source_h source,
                       midsx_tallies_h tallies, uint64_t seed, uint64_t first, uint64_t n, int precision,
-                      void* dst);
+                      void* dst, uint32_t* step_cap = nullptr);
 
 // One batched launch over n_jobs records at `dev_jobs` with history offsets `dev_prefix`
 // (n_jobs + 1 words, last = total) and a history counter `dev_counter` zeroed here, on `s`.
 // spectra: some job's tallies keep an incident-energy spectrum (tallies_spectra), which the
-// lane-parking kernel scores.
+// lane-parking kernel scores.  step_cap: the launch's default per-history step cap (the
+// largest of its jobs' pack_job caps), used when cfg.max_steps is 0.
 midsx_status launch_packed(midsx_tables_h tables, const void* dev_jobs, int n_jobs,
                            const unsigned long long* dev_prefix, unsigned long long total,
                            unsigned long long* dev_counter, const midsx_run_config& cfg, cudaStream_t s,
-                           bool spectra = false);
+                           bool spectra = false, uint32_t step_cap = 100000);
 bool tallies_spectra(midsx_tallies_h t);
 
 // Device bytes the tallies of (specs, dose_mode) take for a phantom of n_voxels voxels.

@@ -347,17 +347,20 @@ bool midsx_gpu_server::launch_locked(bool setup_pending) {
         unsigned long long total = 0;
         s.host_prefix[0] = 0;
         int nj = 0;
+        uint32_t step_cap = 0;
         for (Request* r : cand) {
             const uint64_t n = give[r];
+            uint32_t job_cap = 0;
             midsx_status ps = midsx::rt::pack_job(tables, phantoms[size_t(r->r.phantom)]->h, r->r.source, r->tallies,
                                                   r->r.seed, r->r.first_history + r->scheduled, n, precision,
-                                                  s.host_jobs + size_t(nj) * rec);
+                                                  s.host_jobs + size_t(nj) * rec, &job_cap);
             if (ps != MIDSX_OK) {
                 fail_locked(r, ps, midsx::last_error());
                 changed = true;
                 continue;
             }
             total += n;
+            step_cap = std::max(step_cap, job_cap);
             s.host_prefix[nj + 1] = total;
             s.parts.push_back({r, n});
             ++nj;
@@ -375,7 +378,7 @@ bool midsx_gpu_server::launch_locked(bool setup_pending) {
         bool spectra = false;
         for (auto& p : s.parts) spectra |= midsx::rt::tallies_spectra(p.req->tallies);
         midsx_status ls = good ? midsx::rt::launch_packed(tables, s.dev_jobs, nj, s.dev_prefix, total, s.dev_counter, c,
-                                                          s.stream, spectra)
+                                                          s.stream, spectra, step_cap)
                                : MIDSX_CUDA_ERROR;
         if (ls == MIDSX_OK) good = ok(cudaEventRecord(s.end, s.stream), "cudaEventRecord");
         if (ls != MIDSX_OK || !good) {

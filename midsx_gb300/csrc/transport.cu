@@ -101,6 +101,7 @@ struct DevJob {
     unsigned long long* dose;
     unsigned long long* stats;  // kStCount counters of this job
     uint64_t seed, first, n;
+    uint32_t step_cap;  // default per-history step cap of this job (derived_step_cap)
 };
 
 // Geometry of one job in the working precision (ComputationalDomain with one voxel grid).
@@ -550,6 +551,7 @@ struct midsx_gpu_tables {
     int device = 0;
     int sm_count = 0;
     size_t max_smem = 0;  // opt-in shared memory of one block
+    std::vector<double> maj_x, maj_mu;  // host copy of the majorant's nodes (eV, 1/cm)
 };
 
 struct midsx_gpu_phantom {
@@ -568,6 +570,7 @@ struct midsx_gpu_source {
     DevSource S;
     double* buf = nullptr;
     double max_energy = 0;
+    double min_energy = 0;  // lowest energy the source emits (a bin of non-zero weight)
 };
 
 struct midsx_gpu_tallies {
@@ -761,6 +764,10 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
     T.alpha_f = float(T.alpha);
     T.e_max = blob->e_max;
     fill_lin(T.majorant, blob->majorant);
+    for (int32_t i = 0; i < blob->majorant.n; ++i) {
+        h->maj_x.push_back(blob->data[blob->majorant.x + i]);
+        h->maj_mu.push_back(std::pow(10.0, blob->data[blob->majorant.ly + i]));
+    }
     for (int m = 0; m < blob->n_materials; ++m) {
         const midsx_material_table& s = blob->mat[m];
         DevMaterial& d = T.mat[m];
@@ -1124,13 +1131,16 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
         double sum = 0;
         for (int i = 0; i < nb; ++i) sum += spec->bin_prob[i];
         double acc = 0;
+        s->min_energy = INFINITY;
         for (int i = 0; i < nb; ++i) {
             double p = (sum != 1.0) ? spec->bin_prob[i] / sum : spec->bin_prob[i];
             acc = (i == 0) ? p : acc + p;
             h[i] = spec->bin_energy[i];
             h[nb + i] = acc;
             s->max_energy = std::max(s->max_energy, spec->bin_energy[i]);
+            if (spec->bin_prob[i] > 0) s->min_energy = std::min(s->min_energy, spec->bin_energy[i]);
         }
+        if (!(s->min_energy < INFINITY)) s->min_energy = s->max_energy;
         // device buffer: FP64 energies and CDF, their FP32 copies, then the guide tables of
         // the FP64 and FP32 CDF searches (the same comparison as the device's lower_index; a
         // CDF that is not monotone keeps the full range in every guide interval)
@@ -1167,6 +1177,7 @@ extern "C" midsx_status midsx_gpu_source_create(const midsx_source_spec* spec, m
             return MIDSX_INVALID_ARG;
         }
         s->max_energy = spec->mono_energy;
+        s->min_energy = spec->mono_energy;
     }
     for (int i = 0; i < 3; ++i) {
         S.f_pos[i] = float(S.pos[i]);
@@ -1352,6 +1363,35 @@ midsx_status check_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_sou
     return MIDSX_OK;
 }
 
+// Default per-history step cap of a job.  The reference's history loop has no cap
+// (src/MIDSX/Core/physics_engine.cpp:22); the device loop needs one so that it always ends, and
+// it must not bias results: a straight flight across the domain at energy E takes on average
+// (domain diagonal) x mu_max(E) Woodcock steps.  The cap allows 16 such crossings at the largest
+// majorant between E_floor = min(1 keV, the source's lowest energy) and the tables' e_max,
+// far beyond what a history reaches: photons scattered down to a few keV are absorbed long
+// before (photoelectric absorption dominates there).  At least 100,000, at most 2^31 - 1.
+uint32_t derived_step_cap(const midsx_gpu_tables* tables, midsx_phantom_h phantom, midsx_source_h source) {
+    const double e_floor = std::min(1e3, source->min_energy > 0 ? source->min_energy : 1e3);
+    const std::vector<double>& x = tables->maj_x;
+    const std::vector<double>& mu = tables->maj_mu;
+    double mu_hi = 0;
+    for (size_t i = 0; i < x.size(); ++i)
+        if (x[i] >= e_floor && x[i] <= tables->T.e_max) mu_hi = std::max(mu_hi, mu[i]);
+    // LogLogLinear value at e_floor itself (between nodes)
+    const size_t k = size_t(std::upper_bound(x.begin(), x.end(), e_floor) - x.begin());
+    if (k == 0 || k >= x.size()) {
+        mu_hi = std::max(mu_hi, k == 0 ? (mu.empty() ? 0.0 : mu.front()) : mu.back());
+    } else {
+        const double t = (std::log10(e_floor) - std::log10(x[k - 1])) / (std::log10(x[k]) - std::log10(x[k - 1]));
+        mu_hi = std::max(mu_hi, std::pow(10.0, std::log10(mu[k - 1]) + t * (std::log10(mu[k]) - std::log10(mu[k - 1]))));
+    }
+    const double* d = phantom->G.domain;
+    const double diag = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double cap = std::ceil(16.0 * diag * mu_hi);
+    if (!(cap > 1e5)) return 100000u;
+    return cap >= 2147483647.0 ? 2147483647u : uint32_t(cap);
+}
+
 void fill_job(DevJob& J, midsx_phantom_h phantom, midsx_source_h source, midsx_tallies_h tallies, uint64_t seed,
               uint64_t first, uint64_t n) {
     J.G = phantom->G;
@@ -1364,6 +1404,7 @@ void fill_job(DevJob& J, midsx_phantom_h phantom, midsx_source_h source, midsx_t
     J.seed = seed;
     J.first = first;
     J.n = n;
+    J.step_cap = derived_step_cap(phantom->tables, phantom, source);
 }
 
 template <typename R, bool MULTI>
@@ -1476,7 +1517,9 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
     }
     P.steps_per_pass = cfg.steps_per_pass > 0 ? cfg.steps_per_pass
                                                : default_steps_per_pass(cfg.precision, cfg.tracking, P.server != 0);
-    P.max_steps = cfg.max_steps > 0 ? cfg.max_steps : 100000;
+    // cfg.max_steps = 0: the cap the caller derived from the jobs' geometry (P.max_steps)
+    if (cfg.max_steps > 0) P.max_steps = cfg.max_steps;
+    if (P.max_steps <= 0) P.max_steps = 100000;
     P.max_trials = cfg.max_compton_trials > 0 ? cfg.max_compton_trials : 100000;
     P.regroup = cfg.regroup > 0 ? std::min(cfg.regroup, 32) : (pool ? 32 : 24);
     P.chunk = cfg.chunk > 0 ? std::min(cfg.chunk, 64) : 1;
@@ -1541,6 +1584,12 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
         return MIDSX_INVALID_ARG;
     }
     if (cfg->n_histories == 0) return MIDSX_OK;
+    // a per-history trace runs the lane-parking kernel, which has reference tracking only:
+    // refuse other tracking before anything is built for it (macro cells allocate)
+    if (trace && cfg->tracking != MIDSX_TRACK_REFERENCE) {
+        set_last_error("a per-history trace runs reference tracking only");
+        return MIDSX_INVALID_ARG;
+    }
     if (cfg->tracking == MIDSX_TRACK_MACRO_CELL) {
         const midsx_status cs = ensure_cells(phantom);
         if (cs != MIDSX_OK) return cs;
@@ -1553,6 +1602,7 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
     P.geo_f = make_geo<float>(P.job0.G);
     P.geo_d = make_geo<double>(P.job0.G);
     P.n_jobs = 1;
+    P.max_steps = int(P.job0.step_cap);
     P.counter = tallies->stats + kStCount;
     P.total = cfg->n_histories;
     P.trace = trace;
@@ -1751,9 +1801,18 @@ extern "C" midsx_status midsx_gpu_run_host(midsx_tables_h tables, const midsx_ge
 extern "C" midsx_status midsx_gpu_trace_deposits(midsx_tables_h tables, midsx_phantom_h phantom,
                                                  midsx_source_h source, const midsx_run_config* cfg,
                                                  double* hist_dep) {
-    if (!tables || !phantom || !source || !cfg || !hist_dep || cfg->n_histories == 0 ||
-        cfg->n_histories > (uint64_t(1) << 28))
+    if (!tables || !phantom || !source || !cfg || !hist_dep) {
+        set_last_error("midsx_gpu_trace_deposits: missing handle or output");
         return MIDSX_INVALID_ARG;
+    }
+    if (cfg->n_histories == 0 || cfg->n_histories > (uint64_t(1) << 28)) {
+        set_last_error("midsx_gpu_trace_deposits: n_histories must be in [1, 2^28]");
+        return MIDSX_INVALID_ARG;
+    }
+    if (cfg->tracking != MIDSX_TRACK_REFERENCE) {
+        set_last_error("midsx_gpu_trace_deposits: a per-history trace runs reference tracking only");
+        return MIDSX_INVALID_ARG;
+    }
     midsx_tallies_h tl = nullptr;
     midsx_status st = midsx_gpu_tallies_create(nullptr, nullptr, 0, 0, &tl);
     if (st != MIDSX_OK) return st;
@@ -1791,26 +1850,14 @@ static __device__ __align__(256) unsigned char midsx_noalloc_scratch[kNoAllocSta
                                                                       kNoAllocMaxHistories * sizeof(double)];
 
 namespace {
-std::mutex g_noalloc_mutex;
-void* g_noalloc_address[256] = {};
-
 // Device address of midsx_noalloc_scratch on the current device.  Host code sees only a
-// host-side stand-in under that name, so the address is asked from the runtime once per
-// device, with that device current, and kept.
+// host-side stand-in under that name, so every call asks the runtime for the address with the
+// caller's device current.  Nothing is cached: after a cudaDeviceReset the library's device
+// code is loaded again, possibly at another address.  The lookup allocates nothing.
 midsx_status noalloc_scratch(void** out) {
-    int dev = 0;
-    CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 256) {
-        set_last_error("device ordinal out of range");
-        return MIDSX_INVALID_ARG;
-    }
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_address[dev]) {
-        void* p = nullptr;
-        if (!cuda_ok(cudaGetSymbolAddress(&p, midsx_noalloc_scratch), "cudaGetSymbolAddress")) return MIDSX_CUDA_ERROR;
-        g_noalloc_address[dev] = p;
-    }
-    *out = g_noalloc_address[dev];
+    void* p = nullptr;
+    if (!cuda_ok(cudaGetSymbolAddress(&p, midsx_noalloc_scratch), "cudaGetSymbolAddress")) return MIDSX_CUDA_ERROR;
+    *out = p;
     return MIDSX_OK;
 }
 }  // namespace
@@ -1824,6 +1871,11 @@ extern "C" midsx_status midsx_gpu_trace_deposits_noalloc(midsx_tables_h tables, 
     }
     if (cfg->n_histories > kNoAllocMaxHistories) {
         set_last_error("midsx_gpu_trace_deposits_noalloc: n_histories exceeds its fixed scratch of 1048576 histories");
+        return MIDSX_INVALID_ARG;
+    }
+    // the trace runs reference tracking only; other modes would build macro cells (cudaMalloc)
+    if (cfg->tracking != MIDSX_TRACK_REFERENCE) {
+        set_last_error("midsx_gpu_trace_deposits_noalloc: reference tracking only (other modes allocate)");
         return MIDSX_INVALID_ARG;
     }
     void* base = nullptr;
@@ -1923,6 +1975,7 @@ void batch_params(const midsx_gpu_batch* b, RunParams& P, const unsigned long lo
     P.total = total;
     P.epoch = b->words + 1;
     for (auto* t : b->tallies) P.spectra |= t->spectra;
+    for (const DevJob& j : b->host_jobs) P.max_steps = std::max(P.max_steps, int(j.step_cap));
 }
 
 midsx_status batch_check_precision(midsx_gpu_batch* b, int precision) {
@@ -2182,7 +2235,7 @@ size_t job_record_bytes() { return sizeof(DevJob); }
 
 midsx_status pack_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_source_h source,
                       midsx_tallies_h tallies, uint64_t seed, uint64_t first, uint64_t n, int precision,
-                      void* dst) {
+                      void* dst, uint32_t* step_cap) {
     if (!tables || !phantom || !source || !tallies || !dst) return MIDSX_INVALID_ARG;
     midsx_status st = check_job(tables, phantom, source, tallies, "job");
     if (st != MIDSX_OK) return st;
@@ -2208,6 +2261,7 @@ midsx_status pack_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_sour
     std::memset(&d, 0, sizeof(d));
     fill_job(d, phantom, source, tallies, seed, first, n);
     std::memcpy(dst, &d, sizeof(d));
+    if (step_cap) *step_cap = d.step_cap;
     return MIDSX_OK;
 }
 
@@ -2216,7 +2270,7 @@ bool tallies_spectra(midsx_tallies_h t) { return t && t->spectra; }
 midsx_status launch_packed(midsx_tables_h tables, const void* dev_jobs, int n_jobs,
                            const unsigned long long* dev_prefix, unsigned long long total,
                            unsigned long long* dev_counter, const midsx_run_config& cfg, cudaStream_t s,
-                           bool spectra) {
+                           bool spectra, uint32_t step_cap) {
     if (!tables || !dev_jobs || !dev_prefix || !dev_counter || n_jobs < 1 || n_jobs > kMaxBatchJobs)
         return MIDSX_INVALID_ARG;
     if (cfg.precision != MIDSX_PREC_FP64 && cfg.precision != MIDSX_PREC_MIXED) {
@@ -2234,6 +2288,7 @@ midsx_status launch_packed(midsx_tables_h tables, const void* dev_jobs, int n_jo
     P.total = total;
     P.spectra = spectra;
     P.server = 1;
+    P.max_steps = int(std::min<uint32_t>(step_cap, 2147483647u));
     return launch_kernel(tables, P, cfg, true, s);
 }
 

@@ -36,7 +36,9 @@
 //   * uniforms in the Philox mode are in (0, 1]; the reference's are in [0, 1);
 //   * a voxel index equal to the grid size (a position exactly on the far face, where
 //     the reference's vector::at throws) is clamped and counted;
-//   * bounded loops: per-history step cap and Compton trial cap, counted;
+//   * bounded loops: per-history step cap (by default far above any real history: 16
+//     crossings of the domain at the largest majorant from 1 keV up) and Compton trial cap,
+//     counted;
 //   * table indices are found by comparing raw energies with the node arrays (the
 //     reference compares their log10; the index agrees except at rounding ties).
 #include <algorithm>
@@ -891,7 +893,25 @@ int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size
     }
     if (out->history_deposit)
         for (uint64_t i = 0; i < n; ++i) out->history_deposit[i] = 0;
-    const int steps_cap = max_steps > 0 ? max_steps : 100000;
+    // the reference's loop has no cap; the oracle's default is the device's derived one: 16
+    // crossings of the domain diagonal at the largest majorant between min(1 keV, the source's
+    // lowest energy) and e_max (at least 100,000), so a hit marks a runaway history, not a cut
+    int steps_cap = max_steps;
+    if (steps_cap <= 0) {
+        double e_lo = src->spectrum_kind == MIDSX_SPEC_POLY ? INF : src->mono_energy;
+        for (int i = 0; src->spectrum_kind == MIDSX_SPEC_POLY && i < src->n_bins; ++i)
+            if (src->bin_prob[i] > 0) e_lo = std::min(e_lo, src->bin_energy[i]);
+        const double e_floor = std::min(1e3, e_lo);
+        const midsx_lin_table& mj = blob->majorant;
+        double mu_hi = data.majorant(e_floor);
+        for (int i = 0; i < mj.n; ++i) {
+            const double e = blob->data[mj.x + i];
+            if (e >= e_floor && e <= blob->e_max) mu_hi = std::max(mu_hi, std::pow(10.0, blob->data[mj.ly + i]));
+        }
+        const Vec3& d = dom.dim_space;
+        const double cap = std::ceil(16.0 * std::sqrt(d.x * d.x + d.y * d.y + d.z * d.z) * mu_hi);
+        steps_cap = !(cap > 1e5) ? 100000 : (cap >= 2147483647.0 ? 2147483647 : int(cap));
+    }
     int progress = 0;
     auto t0 = std::chrono::steady_clock::now();
 #pragma omp parallel num_threads(n_threads)

@@ -95,4 +95,8 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # the reference checkout: the first argument, else the MIDSX_REFERENCE_ROOT environment variable
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MIDSX_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: %s <reference checkout> (or set MIDSX_REFERENCE_ROOT)" % sys.argv[0])
+    main(root)

@@ -327,9 +327,9 @@ def test_error_statuses():
     src = M.Source(position=(5, 5, 0), direction=("beam", (5, 5, 10)), energy=60e3)
     M.run(tables, ph, src, tl, 10_000, seed=1, max_steps=2)
     with pytest.raises(N.MidsxError) as e:
-        tl.stats(allow_cap=False)
+        tl.stats()
     assert e.value.status == N.STEP_CAP
-    st = tl.stats()
+    st = tl.stats(allow_cap=True)
     assert st["step_cap_hits"] > 0 and st["histories"] == 10_000
     with pytest.raises(N.MidsxError) as e:
         M.Source(position=(0, 0, 0), direction=("rect", (0, 0, 1), (1, 0, 0), (1, 1, 0)), energy=60e3)

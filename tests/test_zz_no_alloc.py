@@ -7,7 +7,12 @@ loop that cannot afford the device-wide synchronisation of cudaFree.  For them t
 offers this one entry point, which uses a fixed scratch array compiled into its device code
 instead of cudaMalloc.  This test calls it through the C ABI, twice in a row with different
 inputs, and checks each result against the allocating entry point midsx_gpu_trace_deposits
-on the same inputs; it also checks that a request above the fixed limit is refused.
+on the same inputs; it also checks that a request above the fixed limit, or one asking for a
+tracking mode whose set-up would allocate (macro cells), is refused, and that the device's
+free memory (cudaMemGetInfo, read through torch) is the same before and after warm calls.
+The free-memory reading is coarse - the driver hands out memory in pages, so a small
+allocation can hide in a page already mapped - and backs up, not replaces, the code path:
+the entry point calls no allocating routine.
 """
 import ctypes as C
 
@@ -54,3 +59,29 @@ def test_noalloc_trace_refuses_requests_above_its_limit():
     status = call_noalloc(lib, tables, ph, src, cfg, out)
     assert status == N.INVALID_ARG
     assert b"1048576" in lib.midsx_last_error()
+
+
+def free_bytes():
+    import torch
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
+def test_noalloc_trace_leaves_free_memory_unchanged_and_refuses_allocating_modes():
+    sc = scenes.water_cube(n=64, bins=10)
+    tables, ph, src, _ = sc.build()
+    lib = N.load()
+    n = 400_000
+    out = np.zeros(n)
+    cfg = M.run_config(n, seed=5, precision="mixed")
+    assert call_noalloc(lib, tables, ph, src, cfg, out) == N.OK  # warm: the kernel's module is loaded
+    before = free_bytes()
+    for seed in (6, 7):
+        cfg = M.run_config(n, seed=seed, precision="mixed")
+        assert call_noalloc(lib, tables, ph, src, cfg, out) == N.OK, lib.midsx_last_error()
+    assert free_bytes() == before
+    # macro-cell tracking would build the phantom's cells with cudaMalloc: refused up front
+    cfg = M.run_config(n, seed=8, precision="mixed", tracking="macro_cell")
+    assert call_noalloc(lib, tables, ph, src, cfg, out) == N.INVALID_ARG
+    assert b"reference tracking" in lib.midsx_last_error()
+    assert free_bytes() == before
