@@ -146,12 +146,12 @@ def reference_arm(args, world, rank):
     """CPU restatement of the reference transport, all host threads, bounded samples."""
     if rank != 0:
         return
-    import midsx_gb300 as M
     import oracle
     from midsx_gb300 import build as B, scenes
-    B.build()
-    sc = scenes.cone_beam_dose(n_histories=int(args.histories))
-    blob = M.TableBlob(sc.materials, e_max=sc.e_max)
+    B.build()  # compiles the oracle library (nothing of the product is loaded in this arm)
+    al = oracle.tables.tables((scenes.ALUMINIUM,), 150e3)
+    sc = scenes.cone_beam_dose(n_histories=int(args.histories), al=al)
+    blob = oracle.tables_for(sc)  # the oracle's own table build
     threads = os.cpu_count() or 1
     n = int(min(args.cpu_sample, 4e5))
     times = []
@@ -300,7 +300,7 @@ def main():
         import oracle
         threads = os.cpu_count() or 1
         ncpu = int(args.cpu_sample)
-        r = oracle.run(tables.host, n=ncpu, seed=1, rng=oracle.RNG_MT19937, threads=threads, dose=True,
+        r = oracle.run(oracle.tables_for(sc), n=ncpu, seed=1, rng=oracle.RNG_MT19937, threads=threads, dose=True,
                        **sc.oracle_kwargs())
         so = r["stats"]
         result["cpu_baseline"] = {"value": ncpu / r["run_time"], "unit": UNIT, "cores": threads, "kind": "port",

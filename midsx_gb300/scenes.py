@@ -111,7 +111,8 @@ def ellipsoid_phantom(shape, spacing, seed, n_ellipsoids=40, lead_spheres=0):
 
 def kramers_spectrum(kvp, e_min=10.0, al_mm=2.5, tables=None):
     """Kramers' law N(E) ~ (E0 - E) / E on 1 keV bins e_min..kvp (keV), filtered by al_mm of
-    aluminium with the rebuilt Al attenuation table.  Returns (energies eV, weights)."""
+    aluminium with the rebuilt Al attenuation table (`tables`: any table set whose material 0
+    is aluminium, with .eval; default: built here).  Returns (energies eV, weights)."""
     e_kev = np.arange(e_min, kvp + 0.5, 1.0)
     w = (kvp - e_kev) / e_kev
     blob = tables or api.TableBlob([ALUMINIUM], e_max=max(150e3, kvp * 1e3))
@@ -121,7 +122,8 @@ def kramers_spectrum(kvp, e_min=10.0, al_mm=2.5, tables=None):
 
 
 def cone_beam_dose(n_histories=100_000_000, shape=(128, 256, 256), spacing=0.05, seed=1, source_distance=50.0,
-                   half_angle_deg=10.0, kvp=80.0):
+                   half_angle_deg=10.0, kvp=80.0, al=None):
+    """al: tables holding aluminium first, for the filtration (default: built here)."""
     nz, ny, nx = shape
     ids = ellipsoid_phantom(shape, spacing, seed)
     ext = np.array([nx, ny, nz]) * spacing
@@ -130,7 +132,7 @@ def cone_beam_dose(n_histories=100_000_000, shape=(128, 256, 256), spacing=0.05,
     domain = (ext[0], ext[1], z0 + ext[2] + 1.0)
     src_pos = (ext[0] / 2, ext[1] / 2, 0.5)
     radius = source_distance * np.tan(np.radians(half_angle_deg))
-    spectrum = kramers_spectrum(kvp)
+    spectrum = kramers_spectrum(kvp, tables=al)
     source = dict(position=src_pos, direction=("disc", (ext[0] / 2, ext[1] / 2, z0), (0, 0, 1), radius),
                   spectrum=spectrum)
     return Scene("cone_beam_dose_%dx%dx%d_%gkVp" % (nx, ny, nz, kvp),
@@ -165,7 +167,7 @@ def batch_jobs(n_jobs=64, seed=1, edge_range=(32, 256), kvp_range=(20.0, 120.0),
 
 
 def radiography(n_histories=1_000_000_000, shape=(256, 512, 512), spacing=0.05, seed=1, det_bins=512,
-                det_pitch=0.1, sid=100.0, kvp=100.0, lead_spheres=16):
+                det_pitch=0.1, sid=100.0, kvp=100.0, lead_spheres=16, al=None):
     """Projection radiograph: phantom midway between a point source and a det_bins^2
     detector of det_pitch cm bins at `sid` cm (primary and scattered fluence per bin).  With
     lead_spheres=0 the tables hold the four tissue materials only (no lead majorant)."""
@@ -180,7 +182,7 @@ def radiography(n_histories=1_000_000_000, shape=(256, 512, 512), spacing=0.05, 
     corner = ((width - det) / 2, (width - det) / 2, sid)
     specs = [dict(kind="binned", corner=corner, edge1=(det, 0, 0), edge2=(0, det, 0), nu=det_bins, nv=det_bins)]
     source = dict(position=src_pos, direction=("disc", (width / 2, width / 2, sid), (0, 0, 1), det / 2),
-                  spectrum=kramers_spectrum(kvp))
+                  spectrum=kramers_spectrum(kvp, tables=al))
     materials = [AIR, SOFT_TISSUE, ADIPOSE, CORTICAL_BONE] + ([LEAD] if lead_spheres else [])
     return Scene("radiography_%dx%dx%d_%gkVp" % (nx, ny, nz, kvp), materials, domain, (spacing,) * 3, origin, ids,
                  AIR, source, specs, DOSE_SUM, n_histories, 150e3)

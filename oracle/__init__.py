@@ -6,6 +6,12 @@ CPU baseline.  Nothing in midsx_gb300/ imports this package.
 
 Parity is pinned by the reference's own fixtures where they exist (tests/golden/) and by
 the physics checks in tests/; see oracle.cpp for the deviations forced by testing.
+
+The oracle runs on its own interaction tables (oracle/tables.py restates the reference's
+table construction in numpy from the element data files), never on the product's: run()
+and the samplers take any object with the blob layout of include/midsx_gpu.h (.ptr), and
+tables_for(scene) gives the oracle's tables of a scene.  Only the table-index test hands the
+product's arrays to oracle.table_index, to check the device's searches on identical arrays.
 """
 import ctypes as C
 import os
@@ -14,6 +20,8 @@ import numpy as np
 
 from midsx_gb300 import native as N
 from midsx_gb300.api import geometry_spec, source_spec, tally_specs
+
+from . import tables  # noqa: E402  (the oracle's own table build)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
@@ -202,3 +210,15 @@ def philox(ctr, key):
     o = (C.c_uint32 * 4)()
     lib.oracle_philox(c, k, o)
     return list(o)
+
+
+def tables_for(scene):
+    """The oracle's own tables (oracle.tables.OracleTables) of a scene's material list."""
+    return tables.tables(tuple(int(m) for m in scene.materials), float(scene.e_max))
+
+
+def tables_like(t):
+    """The oracle's own tables of the same materials and e_max as the product's Tables or
+    TableBlob `t` (built by oracle/tables.py, not taken from `t`)."""
+    host = getattr(t, "host", t)
+    return tables.tables(tuple(int(m) for m in host.ids), float(host.e_max))

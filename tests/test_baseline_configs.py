@@ -1,0 +1,247 @@
+"""Parity of the CUDA path with the CPU oracle at the benchmark configurations' own sizes.
+
+* Water cube (100^3 water voxels at 1 mm in a 20 cm air box, 60 keV pencil beam, 100 x 100
+  exit-plane bins, 1e6 histories, seed 1): the plain FP64 kernel equals the oracle on the same
+  Philox streams voxel by voxel, and both precisions agree with an independent oracle run
+  (the reference's mt19937 generator): per-voxel chi-square over voxels above 1 % of the
+  maximum, deposited and transmitted energy within 0.5 %, per-bin chi-square on the exit
+  plane.  Reference loop: src/MIDSX/Core/physics_engine.cpp:17-79, run_simulation.cpp:6-41;
+  exit-plane semantics: surface_tally.cpp:16-34.
+* Cone-beam dose (the full 256 x 256 x 128 phantom at 0.5 mm, 80 kVp, 2e6 histories): both
+  precisions against an independent oracle run - totals, Woodcock steps per history and the
+  per-voxel chi-square.
+* Radiography with lead (512 x 512 x 256 at 0.5 mm with sixteen 2 mm lead spheres, 100 kVp,
+  512 x 512 detector at 100 cm): the FP64 kernel equals the oracle on the same Philox streams
+  (detector images by scatter class), and both precisions agree with an independent oracle
+  run on primary and scattered totals and on a 16 x 16 rebinned detector image
+  (surface_quantity.cpp:49-63 classes).  No history reaches the step cap.
+
+The oracle runs with its own tables (oracle/tables.py restates the reference's table
+construction), so a table-build error of the product would show here as well.
+"""
+import numpy as np
+import pytest
+
+import midsx_gb300 as M
+import oracle
+from midsx_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def z_voxels(s_a, v_a, s_b, v_b, frac=0.01):
+    """z-scores of the voxels above frac x the larger maximum; v_* are the variances of the
+    two sums."""
+    m = max(s_a.max(), s_b.max())
+    sel = (s_a > frac * m) | (s_b > frac * m)
+    return (s_a[sel] - s_b[sel]) / np.sqrt(np.maximum(v_a[sel] + v_b[sel], 1e-300))
+
+
+def assert_chi(z, beyond=0.01, label=""):
+    assert z.size > 50, (label, z.size)
+    assert np.mean(np.abs(z) > 3) < beyond, (label, np.mean(np.abs(z) > 3))
+    # mean z^2 is 1 within its sampling error sqrt(2 / n); a conservative variance estimate
+    # lowers it, so only the upper side is tested
+    assert np.mean(z * z) < 1 + 5 * np.sqrt(2 / z.size), (label, np.mean(z * z))
+
+
+def dose_var(d):
+    return d["var"] if "var" in d else d["sumsq"]
+
+
+def z_bins(e_a, c_a, e_b, c_b, min_count=100):
+    """Per-bin z-scores of two binned energy images (compound-Poisson variance sum^2 / count
+    for each), over bins holding at least min_count crossings in both."""
+    sel = (c_a >= min_count) & (c_b >= min_count)
+    va = e_a[sel] ** 2 / c_a[sel]
+    vb = e_b[sel] ** 2 / c_b[sel]
+    return (e_a[sel] - e_b[sel]) / np.sqrt(va + vb)
+
+
+def rebin(img, k):
+    ny, nx = img.shape[:2]
+    return img.reshape(ny // k, k, nx // k, k, *img.shape[2:]).sum(axis=(1, 3))
+
+
+# ------------------------------------------------------------------- water cube ---
+@pytest.fixture(scope="module")
+def cube():
+    sc = scenes.water_cube()  # 100^3 at 1 mm, 100 x 100 bins
+    assert sc.ids.shape == (100, 100, 100) and sc.specs[0]["nu"] == 100
+    objs = sc.build()
+    blob = oracle.tables_for(sc)
+    return sc, objs, blob
+
+
+def test_water_cube_fp64_equals_oracle_on_same_streams(cube):
+    sc, (tables, ph, src, tl), blob = cube
+    n = 1_000_000
+    tl.reset()
+    M.run(tables, ph, src, tl, n, seed=1, precision="fp64")
+    st = tl.stats()
+    d = tl.dose()
+    be, bc = tl.binned(0)
+    o = oracle.run(blob, n=n, seed=1, **sc.oracle_kwargs())
+    so = o["stats"]
+    assert st["histories"] == so["histories"] == n
+    assert st["step_cap_hits"] == so["step_cap_hits"] == 0
+    # same streams: every count equal but for the rare history that meets a decision within
+    # rounding of the two builds' tables
+    for k in ("steps", "photo", "coherent", "incoherent"):
+        assert abs(st[k] - so[k]) <= 1e-4 * so[k] + 2, k
+    assert st["deposited_grid"] == pytest.approx(so["deposited_grid"], rel=1e-4)
+    assert st["escaped_energy"] == pytest.approx(so["escaped_energy"], rel=1e-4)
+    g, c = d["sum"].ravel(), o["dose"]["sum"].ravel()
+    same = np.abs(g - c) <= 1e-9 * np.maximum(1.0, np.abs(c))
+    assert same.mean() > 0.999, same.mean()
+    oe, oc = o["binned"][0]
+    assert np.mean(bc == oc) > 0.999
+    assert be.sum() == pytest.approx(oe.sum(), rel=1e-4)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_water_cube_against_independent_oracle_full_size(cube, precision):
+    sc, (tables, ph, src, tl), blob = cube
+    n = 1_000_000
+    tl.reset()
+    M.run(tables, ph, src, tl, n, seed=1, precision=precision)
+    st = tl.stats()
+    d = tl.dose()
+    be, bc = tl.binned(0)
+    o = oracle.run(blob, n=n, seed=1, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
+    so = o["stats"]
+    assert st["step_cap_hits"] == 0
+    bal = st["deposited_grid"] + st["deposited_background"] + st["escaped_energy"]
+    assert bal == pytest.approx(st["source_energy"], rel=1e-6)
+    assert abs(st["deposited_grid"] - so["deposited_grid"]) / so["deposited_grid"] < 0.005
+    assert abs(st["escaped_energy"] - so["escaped_energy"]) / so["escaped_energy"] < 0.005
+    oe, oc = o["binned"][0]
+    # transmitted energy on the exit plane (all classes) within 0.5 %
+    assert abs(be.sum() - oe.sum()) / oe.sum() < 0.005
+    assert_chi(z_voxels(d["sum"].ravel(), dose_var(d).ravel(), o["dose"]["sum"].ravel(),
+                        dose_var(o["dose"]).ravel()), label="voxels")
+    zb = z_bins(be.sum(axis=2).ravel(), bc.sum(axis=2).ravel(), oe.sum(axis=2).ravel(), oc.sum(axis=2).ravel())
+    assert_chi(zb, label="exit-plane bins")
+
+
+# -------------------------------------------------------------- cone-beam dose ---
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cone_beam_full_phantom_against_independent_oracle(precision):
+    sc = scenes.cone_beam_dose(n_histories=1)
+    assert sc.ids.shape == (128, 256, 256)
+    tables, ph, src, tl = sc.build()
+    blob = oracle.tables_for(sc)
+    n = 2_000_000
+    M.run(tables, ph, src, tl, n, seed=41, precision=precision)
+    st = tl.stats()
+    d = tl.dose()
+    o = oracle.run(blob, n=n, seed=42, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
+    so = o["stats"]
+    assert st["step_cap_hits"] == 0 and so["step_cap_hits"] == 0
+    assert abs(st["deposited_grid"] - so["deposited_grid"]) / so["deposited_grid"] < 0.005
+    assert abs(st["escaped_energy"] - so["escaped_energy"]) / so["escaped_energy"] < 0.005
+    assert abs(st["steps"] - so["steps"]) / so["steps"] < 0.005
+    assert abs(st["voxel_fetches"] - so["voxel_fetches"]) / so["voxel_fetches"] < 0.005
+    assert_chi(z_voxels(d["sum"].ravel(), dose_var(d).ravel(), o["dose"]["sum"].ravel(),
+                        dose_var(o["dose"]).ravel()), beyond=0.012, label="voxels")
+
+
+# ----------------------------------------------------------- radiography, lead ---
+@pytest.fixture(scope="module")
+def radiograph():
+    sc = scenes.radiography(n_histories=1)
+    assert sc.ids.shape == (256, 512, 512) and int((sc.ids == scenes.LEAD).sum()) > 0
+    objs = sc.build()
+    blob = oracle.tables_for(sc)
+    return sc, objs, blob
+
+
+def test_radiography_fp64_equals_oracle_on_same_streams(radiograph):
+    sc, (tables, ph, src, tl), blob = radiograph
+    n = 20_000
+    tl.reset()
+    M.run(tables, ph, src, tl, n, seed=3, precision="fp64")
+    st = tl.stats()
+    be, bc = tl.binned(0)
+    o = oracle.run(blob, n=n, seed=3, dose=False, **sc.oracle_kwargs())
+    so = o["stats"]
+    oe, oc = o["binned"][0]
+    assert st["step_cap_hits"] == 0 and so["step_cap_hits"] == 0
+    assert abs(st["steps"] - so["steps"]) <= 1e-3 * so["steps"]
+    # detector counts by scatter class: the same photons in the same bins
+    for cls in range(4):
+        assert np.abs(bc[..., cls] - oc[..., cls]).sum() <= 1e-3 * oc[..., cls].sum() + 4, cls
+        assert be[..., cls].sum() == pytest.approx(oe[..., cls].sum(), rel=2e-3, abs=1e-6), cls
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_radiography_against_independent_oracle(radiograph, precision):
+    sc, (tables, ph, src, tl), blob = radiograph
+    n_gpu = 1_000_000 if precision == "fp64" else 4_000_000
+    n_cpu = 100_000
+    tl.reset()
+    M.run(tables, ph, src, tl, n_gpu, seed=11, precision=precision)
+    st = tl.stats()
+    be, bc = tl.binned(0)
+    o = oracle.run(blob, n=n_cpu, seed=12, rng=oracle.RNG_MT19937, dose=False, **sc.oracle_kwargs())
+    so = o["stats"]
+    oe, oc = o["binned"][0]
+    assert st["step_cap_hits"] == 0 and so["step_cap_hits"] == 0
+    # Woodcock steps per history: the same algorithm against the same (lead) majorant
+    assert abs(st["steps"] / n_gpu - so["steps"] / n_cpu) / (so["steps"] / n_cpu) < 0.01
+    # primary and scattered totals per history, within 4 sigma of the two samples (the
+    # oracle's 1e5 histories dominate) - counts per history are binomial-like
+    for name, cls in (("primary", [0]), ("scatter", [1, 2, 3])):
+        cg, co = bc[..., cls].sum() / n_gpu, oc[..., cls].sum() / n_cpu
+        eg, eo = be[..., cls].sum() / n_gpu, oe[..., cls].sum() / n_cpu
+        sig_c = np.sqrt(cg / n_gpu + co / n_cpu)
+        assert abs(cg - co) < 4 * sig_c, (name, cg, co, sig_c)
+        assert abs(eg - eo) / eo < 4 * sig_c / co + 1e-3, (name, eg, eo)
+    # 16 x 16 rebinned image (32 x 32 detector bins each), per class group, per history
+    for cls in ([0], [1, 2, 3]):
+        ig = rebin(be[..., cls].sum(axis=2), 32).ravel() / n_gpu
+        cg = rebin(bc[..., cls].sum(axis=2), 32).ravel()
+        io = rebin(oe[..., cls].sum(axis=2), 32).ravel() / n_cpu
+        co = rebin(oc[..., cls].sum(axis=2), 32).ravel()
+        sel = (cg >= 100) & (co >= 100)
+        z = (ig[sel] - io[sel]) / np.sqrt(ig[sel] ** 2 / cg[sel] + io[sel] ** 2 / co[sel])
+        assert z.size > 20, cls
+        assert np.mean(np.abs(z) > 3) < 0.02, (cls, np.mean(np.abs(z) > 3))
+        assert np.mean(z * z) < 1 + 5 * np.sqrt(2 / z.size), (cls, np.mean(z * z))
+
+
+# ------------------------------------------------------------- isotropic source ---
+def test_isotropic_source_against_oracle():
+    """IsotropicDirectionality (src/MIDSX/Core/source.cpp:62-70: theta ~ U[0, pi],
+    phi ~ U[0, 2 pi), the reference's definition): a point source inside a water cube, FP64
+    per-history deposits equal to the oracle's on the same streams, scalar cuboid tallies
+    and the dose against an independent oracle run."""
+    ids = np.full((40, 40, 40), scenes.WATER, np.uint8)
+    source = dict(position=(10, 10, 10), direction=("isotropic",), energy=50e3)
+    sc = scenes.Scene("isotropic_point_in_water", [scenes.AIR, scenes.WATER], (20, 20, 20), (0.1, 0.1, 0.1),
+                      (8, 8, 8), ids, scenes.AIR, source,
+                      [dict(kind="cuboid", min=(8, 8, 8), max=(10, 12, 12)),
+                       dict(kind="disc", center=(10, 10, 19), normal=(0, 0, 1), radius=5.0)], 2, 1, 100e3)
+    tables, ph, src, tl = sc.build()
+    blob = oracle.tables_for(sc)
+    n = 200_000
+    g = M.trace_deposits(tables, ph, src, n, seed=2, precision="fp64")
+    o = oracle.run(blob, n=n, seed=2, history=True, dose=False, **sc.oracle_kwargs())["history_deposit"]
+    assert np.mean(np.abs(g - o) <= 1e-9 * np.maximum(1.0, o)) > 0.999
+    for precision in ("fp64", "mixed"):
+        tl.reset()
+        M.run(tables, ph, src, tl, n, seed=3, precision=precision)
+        d = tl.dose()
+        oo = oracle.run(blob, n=n, seed=4, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
+        for t in (0, 1):
+            gs, os_ = tl.scalar(t), oo["scalar"][t]
+            # photons counted (all classes): Poisson, within 4 sigma
+            a, b = gs[24:28].sum(), os_[24:28].sum()
+            assert abs(a - b) < 4 * np.sqrt(a + b) + 1, (precision, t, a, b)
+            # first vector quantity (deposited energy of the cuboid, incident energy of the
+            # disc) summed over classes, within 4 sigma from its sums of squares
+            a, b = gs[1:12:3].sum(), os_[1:12:3].sum()
+            va, vb = gs[2:12:3].sum(), os_[2:12:3].sum()
+            assert abs(a - b) < 4 * np.sqrt(va + vb) + 1e-9 * abs(b), (precision, t, a, b)
+        assert_chi(z_voxels(d["sum"].ravel(), dose_var(d).ravel(), oo["dose"]["sum"].ravel(),
+                            dose_var(oo["dose"]).ravel()), beyond=0.015, label=precision)

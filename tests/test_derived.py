@@ -83,7 +83,7 @@ def test_mu_en_incoherent_share_matches_compton_sampler(energy):
     photo = blob.eval(0, "photo", [energy])[0]
     incoh = blob.eval(0, "incoherent", [energy])[0]
     f = (mu_en * rho - photo) / incoh
-    _, kp = oracle.sample(blob, "compton", 0, energy, 200_000, seed=9)
+    _, kp = oracle.sample(oracle.tables_like(blob), "compton", 0, energy, 200_000, seed=9)
     share = 1 - kp
     assert abs(share.mean() - f) < 4 * share.std() / math.sqrt(share.size), (share.mean(), f)
 
@@ -122,7 +122,7 @@ def test_spectrum_derived_quantities_equal_raw_vector_algorithm(golden, case):
     tally = hvl_tally(golden, src)
     ids, spacing = hvl_geometry(golden, case, "hvl")
     sc = golden["scene"]
-    o = oracle.run(blob, sc["domain"], spacing, sc["slab_origin"], ids, scenes.AIR, src, [tally], n=20_000, seed=4,
+    o = oracle.run(oracle.tables_like(blob), sc["domain"], spacing, sc["slab_origin"], ids, scenes.AIR, src, [tally], n=20_000, seed=4,
                    raw_spec=0, dose=False)
     raw_e, raw_c = o["raw"]
     count, cosine = o["spectrum"][0]
@@ -157,7 +157,7 @@ def test_oracle_polyenergetic_hvl_through_spectrum_air_kerma(golden, case):
     ak, prim = {}, {}
     for kind, seed in (("0", 21), ("hvl", 22), ("qvl", 23)):
         ids, spacing = hvl_geometry(golden, case, kind)
-        o = oracle.run(blob, sc["domain"], spacing, sc["slab_origin"], ids, scenes.AIR, src, [tally], n=n, seed=seed,
+        o = oracle.run(oracle.tables_like(blob), sc["domain"], spacing, sc["slab_origin"], ids, scenes.AIR, src, [tally], n=n, seed=seed,
                        dose=False)
         count, cosine = o["spectrum"][0]
         mu = blob.mu_en(air, MIDPOINTS)
@@ -190,7 +190,7 @@ def test_gpu_spectrum_equals_oracle_fp64(golden, case):
     tl = M.Tallies(ph, [tally], N.DOSE_OFF)
     M.run(tables, ph, M.Source(**src_d), tl, n, seed=31, precision="fp64")
     count, cosine = tl.spectrum(0)
-    o = oracle.run(tables.host, sc["domain"], spacing, sc["slab_origin"], ids, scenes.AIR, src_d, [tally], n=n,
+    o = oracle.run(oracle.tables_like(tables), sc["domain"], spacing, sc["slab_origin"], ids, scenes.AIR, src_d, [tally], n=n,
                    seed=31, dose=False)
     oc, os_ = o["spectrum"][0]
     assert oc.sum() > 0.3 * n

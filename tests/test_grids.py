@@ -36,7 +36,7 @@ MATERIALS = [scenes.AIR, scenes.WATER, scenes.SOFT_TISSUE, scenes.LEAD]
 
 def test_oracle_single_grid_list_equals_single_grid():
     sc = scenes.water_cube(n_histories=1, n=20, bins=4)
-    blob = M.TableBlob(sc.materials, e_max=sc.e_max)
+    blob = oracle.tables_for(sc)
     kw = sc.oracle_kwargs()
     a = oracle.run(blob, n=20_000, seed=3, threads=2, **kw)
     b = oracle.run(blob, n=20_000, seed=3, threads=2, grids=[(sc.ids, sc.spacing, sc.origin)], **kw)
@@ -49,7 +49,7 @@ def test_oracle_first_grid_wins():
     """A second grid lying wholly inside the first is never reached: the transport equals the
     first grid alone, and the second grid's dose stays zero."""
     sc = scenes.water_cube(n_histories=1, n=20, bins=4)
-    blob = M.TableBlob(sc.materials, e_max=sc.e_max)
+    blob = oracle.tables_for(sc)
     kw = sc.oracle_kwargs()
     inner = np.full((4, 4, 4), scenes.AIR, dtype=np.uint8)
     a = oracle.run(blob, n=20_000, seed=4, threads=2, **kw)
@@ -68,7 +68,7 @@ def test_grids_fp64_histories_equal_oracle():
     src = M.Source(**source)
     n = 60_000
     g = M.trace_deposits(tables, ph, src, n, seed=12, precision="fp64")
-    o = oracle.run(tables.host, domain, None, None, None, scenes.AIR, source, n=n, seed=12, history=True,
+    o = oracle.run(oracle.tables_like(tables), domain, None, None, None, scenes.AIR, source, n=n, seed=12, history=True,
                    dose=False, grids=grids)["history_deposit"]
     same = np.abs(g - o) <= 1e-9 * np.maximum(1.0, np.abs(o))
     assert o.sum() > 0 and same.mean() > 0.999, same.mean()
@@ -87,7 +87,7 @@ def test_grids_dose_against_oracle(precision):
     M.run(tables, ph, src, tl, n, seed=5, precision=precision)
     d = tl.dose()
     st = tl.stats()
-    o = oracle.run(tables.host, domain, None, None, None, scenes.AIR, source, n=n, seed=6, rng=oracle.RNG_MT19937,
+    o = oracle.run(oracle.tables_like(tables), domain, None, None, None, scenes.AIR, source, n=n, seed=6, rng=oracle.RNG_MT19937,
                    grids=grids)
     assert len(d["sum"]) == 3 and d["sum"][2].shape == grids[2][0].shape
     # all grids together: most of the deposit is whole-photon absorption in lead, so the

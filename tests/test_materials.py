@@ -57,7 +57,7 @@ def test_fp64_histories_equal_oracle_with_twenty_materials(case5):
     sc, (tables, ph, src, tl) = case5
     n = 40_000
     g = M.trace_deposits(tables, ph, src, n, seed=8, precision="fp64")
-    o = oracle.run(tables.host, n=n, seed=8, history=True, dose=False, **sc.oracle_kwargs())["history_deposit"]
+    o = oracle.run(oracle.tables_like(tables), n=n, seed=8, history=True, dose=False, **sc.oracle_kwargs())["history_deposit"]
     same = np.abs(g - o) <= 1e-9 * np.maximum(1.0, np.abs(o))
     assert same.mean() > 0.999, same.mean()
     assert g.sum() > 0

@@ -8,7 +8,9 @@ Pins of the oracle:
 * the two RNG modes (per-history Philox, per-thread mt19937 as in the reference) agree
   statistically.
 Table-builder checks restate the reference's table arithmetic in numpy from the raw
-element data (epdl_photon.bin), independently of the C++ builder.
+element data (epdl_photon.bin), independently of the C++ builder; the oracle's own table
+build (oracle/tables.py) is compared with the product's array by array, and the oracle runs
+on its own tables throughout.
 """
 import math
 import os
@@ -65,7 +67,7 @@ def ratio_sigma(n_a, n_b, n):
 def test_oracle_reproduces_reference_hvl(golden, case):
     """Primary air-kerma ratios AK_hvl/AK_0 and AK_qvl/AK_0 of the reference's own runs
     (mono-energetic: the ratio of primary photon counts on the disc)."""
-    blob = M.TableBlob([scenes.AIR, scenes.ALUMINIUM], e_max=150e3)
+    blob = oracle.tables.tables((scenes.AIR, scenes.ALUMINIUM), 150e3)
     n = 200_000
     n0 = hvl_primary(blob, golden, case, "0", n, 11)
     ref = golden["cases"][case]
@@ -79,7 +81,7 @@ def test_oracle_reproduces_reference_hvl(golden, case):
 
 def test_rng_modes_agree_statistically():
     sc = scenes.water_cube(n=20, bins=10)
-    blob = M.TableBlob(sc.materials, e_max=sc.e_max)
+    blob = oracle.tables_for(sc)
     a = oracle.run(blob, n=100_000, seed=3, rng=oracle.RNG_PHILOX, **sc.oracle_kwargs())["stats"]
     b = oracle.run(blob, n=100_000, seed=3, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())["stats"]
     for k in ("photo", "coherent", "incoherent"):
@@ -90,7 +92,7 @@ def test_rng_modes_agree_statistically():
 
 def test_split_history_ranges_equal_one_run():
     sc = scenes.water_cube(n=10, bins=10)
-    blob = M.TableBlob(sc.materials, e_max=sc.e_max)
+    blob = oracle.tables_for(sc)
     one = oracle.run(blob, n=4000, seed=5, history=True, **sc.oracle_kwargs())
     lo = oracle.run(blob, n=2000, seed=5, first=0, history=True, **sc.oracle_kwargs())
     hi = oracle.run(blob, n=2000, seed=5, first=2000, history=True, **sc.oracle_kwargs())
@@ -173,35 +175,90 @@ def test_total_is_sum_of_components_and_majorant_dominates():
         assert np.all(blob.eval(0, "majorant", e) >= tot * (1 - 1e-9))
 
 
-def test_spline_interpolates_its_nodes_and_matches_scipy():
-    """LogLogSpline (Eigen SplineFitting, knot averaging) rebuilt from The NURBS Book: the
-    curve passes through its data points, and scipy's BSpline with the same knots and
-    coefficients solved densely gives the same values."""
-    from scipy.interpolate import BSpline
-    from scipy.linalg import solve
-    blob = M.TableBlob([scenes.WATER], e_max=150e3)
-    t = blob.blob.mat[0].coh
-    knots = blob.array(t.knot_u, t.n_ctrl + t.degree + 1)
-    ctrl = blob.array(t.ctrl, t.n_ctrl)
-    # rebuild the coefficients with a dense solve from the node data (u_i, log10 y_i)
+TABLE_MATERIALS = [scenes.AIR, scenes.WATER, scenes.SOFT_TISSUE, scenes.ADIPOSE, scenes.CORTICAL_BONE,
+                   scenes.ALUMINIUM, scenes.LEAD]
+
+
+def test_product_tables_equal_the_oracles_independent_build():
+    """The product's C++ table build (midsx_gb300/csrc/tables.cpp) against the oracle's own
+    numpy restatement of the reference's construction (oracle/tables.py), array by array:
+    every node grid and RITA energy grid bit-identical, log10 values within 1e-12, spline
+    control points within 1e-9 (two different solvers of the collocation system), RITA rows
+    of equal length with y within 1e-13 and the interpolation parameters a, b within 1e-8
+    (they come from a difference of nearly equal slopes); evaluated values within 1e-10."""
+    p = M.TableBlob(TABLE_MATERIALS, e_max=150e3)
+    o = oracle.tables.OracleTables(TABLE_MATERIALS, 150e3)
+
+    def lin(tp, to):
+        assert tp.n == to.n
+        np.testing.assert_array_equal(p.array(tp.x, tp.n), o.array(to.x, to.n))
+        for f in ("lx", "ly"):
+            a, b = p.array(getattr(tp, f), tp.n), o.array(getattr(to, f), to.n)
+            fin = np.isfinite(a)
+            np.testing.assert_array_equal(fin, np.isfinite(b))
+            np.testing.assert_allclose(b[fin], a[fin], rtol=0, atol=1e-12)
+
+    lin(p.blob.majorant, o.blob.majorant)
+    rng = np.random.default_rng(7)
+    e = np.exp(rng.uniform(np.log(1e3), np.log(1.5e5), 2000))
+    np.testing.assert_allclose(o.eval(0, "majorant", e), p.eval(0, "majorant", e), rtol=1e-10)
+    for m in range(len(TABLE_MATERIALS)):
+        tp, to = p.blob.mat[m], o.blob.mat[m]
+        assert tp.id == to.id and tp.density == to.density
+        for name in ("total", "photo", "sfunc", "ffactor"):
+            lin(getattr(tp, name), getattr(to, name))
+        for name in ("coh", "incoh"):
+            sp, so = getattr(tp, name), getattr(to, name)
+            assert (sp.n_ctrl, sp.degree) == (so.n_ctrl, so.degree)
+            assert sp.lx_min == so.lx_min and sp.lx_max == so.lx_max
+            nk = sp.n_ctrl + sp.degree + 1
+            np.testing.assert_allclose(o.array(so.knot_u, nk), p.array(sp.knot_u, nk), rtol=0, atol=1e-15)
+            np.testing.assert_allclose(o.array(so.ctrl, so.n_ctrl), p.array(sp.ctrl, sp.n_ctrl), rtol=0, atol=1e-9)
+        for which in ("total", "photo", "coherent", "incoherent"):
+            np.testing.assert_allclose(o.eval(m, which, e), p.eval(m, which, e), rtol=1e-10, err_msg=which)
+        rp, ro = tp.rita, to.rita
+        assert (rp.n_energy, rp.n_rows) == (ro.n_energy, ro.n_rows)
+        np.testing.assert_array_equal(p.array(rp.energy, rp.n_energy), o.array(ro.energy, ro.n_energy))
+        np.testing.assert_array_equal(p.iarray(rp.row_start, rp.n_energy + 1), o.iarray(ro.row_start, ro.n_energy + 1))
+        np.testing.assert_array_equal(p.array(rp.x, rp.n_rows), o.array(ro.x, ro.n_rows))
+        for f, tol in (("y", 1e-13), ("a", 1e-8), ("b", 1e-8)):
+            a, b = p.array(getattr(rp, f), rp.n_rows), o.array(getattr(ro, f), ro.n_rows)
+            fin = np.isfinite(a)
+            np.testing.assert_array_equal(fin, np.isfinite(b))
+            np.testing.assert_allclose(b[fin], a[fin], rtol=tol, atol=tol, err_msg=f)
+
+
+def test_spline_collocation_solved_from_raw_epdl_nodes():
+    """Water's coherent LogLogSpline rebuilt from the raw EPDL nodes without either builder:
+    the element tables of H and O (epdl_photon.bin) through the element splines (scipy's
+    make_interp_spline with the averaged knots, a banded solver of its own), weighted by the
+    number densities on the merged grid, and the material spline solved again by scipy.  The
+    product's table gives the same values at the nodes and between them."""
+    from scipy.interpolate import make_interp_spline
     data = read_epdl(os.path.join(M.DATA_DIR, "epdl_photon.bin"))
+    blob = M.TableBlob([scenes.WATER], e_max=150e3)
+
+    def loglog_spline(x, y):
+        lx, ly = np.log10(x), np.log10(y)
+        lo, hi = lx.min(), lx.max()
+        u = (lx - lo) / (hi - lo)
+        p = min(x.size - 1, 3)
+        t = np.zeros(x.size + p + 1)
+        for j in range(1, x.size - p):
+            t[j + p] = u[j:j + p].mean()
+        t[x.size:] = 1.0
+        b = make_interp_spline(u, ly, k=p, t=t)
+        return lambda q: 10 ** b((np.log10(q) - lo) / (hi - lo))
+
     w = {1: 0.111898, 8: 0.888102}
-    n_d = {z: 6.022140857e23 * 1.0 * w[z] / {1: 1.00794, 8: 15.9994}[z] for z in w}
+    awt = {1: 1.00794, 8: 15.9994}
     grid = np.unique(np.concatenate([data[z][0][0] for z in w]))
-    assert grid.size == t.n_ctrl
-    u = (np.log10(grid) - t.lx_min) / (t.lx_max - t.lx_min)
-    A = BSpline.design_matrix(np.clip(u, 0, 1 - 1e-15), knots, t.degree).toarray()
-    A[-1, :] = 0
-    A[-1, -1] = 1
-    curve = BSpline(knots, ctrl, t.degree, extrapolate=True)
-    vals = curve(u)
-    # the material table values y_i are reproduced at the nodes
-    y_nodes = blob.eval(0, "coherent", grid)
-    np.testing.assert_allclose(np.log10(y_nodes), vals, rtol=0, atol=1e-9)
-    # a dense solve of the same collocation system gives the same control points
-    c2 = solve(A, vals)
-    np.testing.assert_allclose(c2, ctrl, rtol=0, atol=1e-7)
-    assert n_d  # element number densities used by the builder are positive
+    y = sum(6.022140857e23 * 1.0 * w[z] / awt[z] * loglog_spline(*data[z][0])(grid) for z in w) * 1e-24
+    coh = loglog_spline(grid, y)
+    np.testing.assert_allclose(blob.eval(0, "coherent", grid), y, rtol=1e-9)
+    q = np.sqrt(grid[1:] * grid[:-1])
+    q = q[(q > 1e3) & (q < 1.5e5)]
+    np.testing.assert_allclose(blob.eval(0, "coherent", q), coh(q), rtol=1e-9)
 
 
 ALPHA = 0.51099895000E6 / (math.sqrt(2.0) * 4.135667662e-15 * 299792458E2 * 1E8)

@@ -70,7 +70,7 @@ def test_fast_cone_beam_crop_against_oracle(precision, tracking):
     n = 300_000
     tl = run(tables, ph, src, [], n, 31, precision, tracking)
     st, d = tl.stats(), tl.dose()
-    o = oracle.run(tables.host, n=n, seed=32, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
+    o = oracle.run(oracle.tables_like(tables), n=n, seed=32, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
     so = o["stats"]
     assert st["steps"] < 0.35 * so["steps"], (st["steps"], so["steps"])
     q = d["sumsq"].sum() + o["dose"]["sumsq"].sum()
@@ -91,7 +91,7 @@ def test_fast_multi_grid_against_oracle(tracking):
     n = 300_000
     tl = run(tables, ph, src, [], n, 7, "mixed", tracking)
     d, st = tl.dose(), tl.stats()
-    o = oracle.run(tables.host, domain, None, None, None, scenes.AIR, source, n=n, seed=8, rng=oracle.RNG_MT19937,
+    o = oracle.run(oracle.tables_like(tables), domain, None, None, None, scenes.AIR, source, n=n, seed=8, rng=oracle.RNG_MT19937,
                    grids=grids)
     for k in range(3):
         gs, os_ = d["sum"][k].sum(), o["dose"]["sum"][k].sum()
