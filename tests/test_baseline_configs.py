@@ -174,8 +174,16 @@ def test_radiography_fp64_equals_oracle_on_same_streams(radiograph):
         assert be[..., cls].sum() == pytest.approx(oe[..., cls].sum(), rel=2e-3, abs=1e-6), cls
 
 
+@pytest.fixture(scope="module")
+def radiograph_oracle(radiograph):
+    """One independent oracle run (mt19937) shared by both precisions: 1e5 histories at
+    ~17.5k Woodcock steps each."""
+    sc, _, blob = radiograph
+    return oracle.run(blob, n=100_000, seed=12, rng=oracle.RNG_MT19937, dose=False, **sc.oracle_kwargs())
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_radiography_against_independent_oracle(radiograph, precision):
+def test_radiography_against_independent_oracle(radiograph, radiograph_oracle, precision):
     sc, (tables, ph, src, tl), blob = radiograph
     n_gpu = 1_000_000 if precision == "fp64" else 4_000_000
     n_cpu = 100_000
@@ -183,7 +191,7 @@ def test_radiography_against_independent_oracle(radiograph, precision):
     M.run(tables, ph, src, tl, n_gpu, seed=11, precision=precision)
     st = tl.stats()
     be, bc = tl.binned(0)
-    o = oracle.run(blob, n=n_cpu, seed=12, rng=oracle.RNG_MT19937, dose=False, **sc.oracle_kwargs())
+    o = radiograph_oracle
     so = o["stats"]
     oe, oc = o["binned"][0]
     assert st["step_cap_hits"] == 0 and so["step_cap_hits"] == 0
