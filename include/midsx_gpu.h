@@ -264,8 +264,21 @@ typedef enum midsx_tally_kind {
 typedef enum midsx_dose_mode {
     MIDSX_DOSE_OFF = 0,
     MIDSX_DOSE_SUM = 1,      /* energy sum per voxel only */
-    MIDSX_DOSE_FULL = 2      /* count, sum and sum of squares per voxel */
+    MIDSX_DOSE_FULL = 2,     /* count, sum and sum of squares per voxel */
+    MIDSX_DOSE_BATCHES = 3   /* FULL plus the batch-method variance of each voxel's sum */
 } midsx_dose_mode;
+
+/* Batch-method variance (MIDSX_DOSE_BATCHES).  The reference's per-voxel sigma
+ * (src/MIDSX/Core/quantity.cpp:37-45) is the spread of single deposits, which is not the
+ * uncertainty of a voxel's dose when a history deposits more than once in the voxel.  The batch
+ * method is: a run of N histories is split into B batches of (nearly) N / B histories - disjoint
+ * history-id ranges, so independent - and the variance of a voxel's total is B s^2, s^2 the
+ * sample variance of its B batch sums.  Each midsx_gpu_run into such tallies closes one batch
+ * at its end, or cfg->variance_batches batches when that is 2 or more (the run is split into
+ * that many launches over consecutive history ranges); the batch sums are folded into a running
+ * mean and sum of squared deviations per voxel (Welford) on the device.  Batched launches do not
+ * close batches, and the request server does not take this mode.  The tallies take 16 more
+ * bytes per voxel. */
 
 #define MIDSX_MAX_ENERGY_BINS 65536
 
@@ -346,6 +359,9 @@ typedef struct midsx_run_config {
                                     default: 2 for the FP32 form with reference tracking, else
                                     1; the request server's default is 1).  Single runs use
                                     the default, fixed at compile time. */
+    int32_t variance_batches;    /* MIDSX_DOSE_BATCHES tallies: batches this run is split into
+                                    (0 or 1: the run is one batch); at most 1024 */
+    int32_t reserved;
     uint64_t seed;
     uint64_t first_history;      /* history ids [first, first + n) select Philox streams */
     uint64_t n_histories;
@@ -377,6 +393,10 @@ midsx_status midsx_gpu_fetch_stats(midsx_tallies_h t, midsx_run_stats* out, void
 /* Voxel dose: any of the three outputs may be NULL; each has n_voxels entries. */
 midsx_status midsx_gpu_fetch_dose(midsx_tallies_h t, double* sum, double* sumsq, double* count,
                                   void* stream);
+/* Batch-method variance of each voxel's dose sum (MIDSX_DOSE_BATCHES tallies, at least two
+ * batches closed): var[n_voxels] = B / (B - 1) * sum_b (S_b - S / B)^2 over the B batch sums
+ * S_b, eV^2; *n_batches (may be NULL) receives B.  Synchronises `stream`. */
+midsx_status midsx_gpu_fetch_dose_variance(midsx_tallies_h t, double* var, int32_t* n_batches, void* stream);
 /* Scalar tally `index` (0-based among the specs): MIDSX_SCALAR_SLOTS doubles, layout
  * [q][class][n, sum, sumsq] for the two vector quantities (24 values) followed by
  * [q][class] counts for the count quantities (8 values; surfaces use the first 4). */

@@ -302,10 +302,13 @@ class Tallies:
 
     def dose(self, stream=None):
         """Per-voxel dose records: arrays shaped like the phantom's grid, or, for a phantom of
-        several grids, lists with one array per grid."""
+        several grids, lists with one array per grid.  "sum" (eV); with DOSE_FULL or
+        DOSE_BATCHES also the reference's per-deposit "sumsq" and "count"; with DOSE_BATCHES
+        and at least two batches closed also "var", the batch-method variance of each voxel's
+        sum (eV^2), and "batches"."""
         n = int(sum(np.prod(sh) for sh in self.shapes))
         s = np.empty(n)
-        full = self.dose_mode == N.DOSE_FULL
+        full = self.dose_mode in (N.DOSE_FULL, N.DOSE_BATCHES)
         s2 = np.empty(n) if full else None
         c = np.empty(n) if full else None
         N.check(N.load().midsx_gpu_fetch_dose(self.handle, N.dptr(s), N.dptr(s2) if full else None,
@@ -324,6 +327,15 @@ class Tallies:
         if full:
             out["sumsq"] = shaped(s2)
             out["count"] = shaped(c)
+        if self.dose_mode == N.DOSE_BATCHES:
+            v = np.empty(n)
+            b = C.c_int32()
+            st = N.load().midsx_gpu_fetch_dose_variance(self.handle, N.dptr(v), C.byref(b), stream)
+            if st == N.OK:
+                out["var"] = shaped(v)
+                out["batches"] = b.value
+            elif st != N.INVALID_ARG:  # fewer than two batches: no variance yet
+                N.check(st, "midsx_gpu_fetch_dose_variance")
         return out
 
     def scalar(self, i, stream=None):
@@ -374,8 +386,9 @@ TRACKING = {"reference": N.TRACK_REFERENCE, "background_fast": N.TRACK_BACKGROUN
 
 
 def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0, regroup=0,
-               chunk=0, scheduler="default", tracking="reference", steps_per_pass=0):
+               chunk=0, scheduler="default", tracking="reference", steps_per_pass=0, variance_batches=0):
     c = N.RunConfig()
+    c.variance_batches = int(variance_batches)
     c.steps_per_pass = int(steps_per_pass)
     c.tracking = TRACKING[tracking] if isinstance(tracking, str) else int(tracking)
     c.regroup = int(regroup)

@@ -586,6 +586,10 @@ struct midsx_gpu_tallies {
     int precision = -1;   // precision of the accumulated contents, -1 = empty
     bool pooled = false;  // one pool block starting at `stats`, owned by a request server
     bool spectra = false; // some surface tally keeps an incident-energy spectrum
+    // MIDSX_DOSE_BATCHES: per voxel the running mean and sum of squared deviations of the
+    // batch sums (Welford); each dose record's fourth word holds the sum at the last close
+    double* batch = nullptr;
+    int batches_closed = 0;
 };
 
 namespace {
@@ -1206,7 +1210,8 @@ namespace {
 // sizes.  Allocates nothing on the device.
 midsx_status tallies_layout(size_t n_voxels, const midsx_tally_spec* specs, int32_t n_specs, int32_t dose_mode,
                             midsx_gpu_tallies* t) {
-    if (n_specs < 0 || n_specs > MIDSX_MAX_TALLIES || (n_specs > 0 && !specs) || dose_mode < 0 || dose_mode > 2) {
+    if (n_specs < 0 || n_specs > MIDSX_MAX_TALLIES || (n_specs > 0 && !specs) || dose_mode < 0 ||
+        dose_mode > MIDSX_DOSE_BATCHES) {
         set_last_error("midsx_gpu_tallies_create: invalid argument");
         return MIDSX_INVALID_ARG;
     }
@@ -1284,7 +1289,7 @@ midsx_status tallies_layout(size_t n_voxels, const midsx_tally_spec* specs, int3
 // tally records and the dose grid.
 size_t tallies_bytes(const midsx_gpu_tallies* t) {
     return (kStCount + 1) * 8 + t->acc_words * 8 + t->host_specs.size() * sizeof(DevTally) +
-           t->n_voxels * size_t(t->dose_stride) * 8;
+           t->n_voxels * size_t(t->dose_stride) * 8 + (t->dose_mode == MIDSX_DOSE_BATCHES ? t->n_voxels * 16 : 0);
 }
 
 }  // namespace
@@ -1305,7 +1310,8 @@ extern "C" midsx_status midsx_gpu_tallies_create(midsx_phantom_h phantom, const 
         (words && !cuda_ok(cudaMalloc(&t->acc, words * 8), "cudaMalloc")) ||
         (n_specs && !cuda_ok(cudaMalloc(&t->specs, n_specs * sizeof(DevTally)), "cudaMalloc")) ||
         (t->dose_stride &&
-         !cuda_ok(cudaMalloc(&t->dose, t->n_voxels * t->dose_stride * sizeof(unsigned long long)), "cudaMalloc")))
+         !cuda_ok(cudaMalloc(&t->dose, t->n_voxels * t->dose_stride * sizeof(unsigned long long)), "cudaMalloc")) ||
+        (dose_mode == MIDSX_DOSE_BATCHES && !cuda_ok(cudaMalloc(&t->batch, t->n_voxels * 16), "cudaMalloc")))
         return MIDSX_OOM;
     for (auto& d : t->host_specs) d.acc = t->acc + reinterpret_cast<size_t>(d.acc);
     if (n_specs)
@@ -1325,6 +1331,7 @@ extern "C" midsx_status midsx_gpu_tallies_destroy(midsx_tallies_h t) {
         return MIDSX_INVALID_ARG;
     }
     cudaFree(t->dose);
+    cudaFree(t->batch);
     cudaFree(t->specs);
     cudaFree(t->acc);
     cudaFree(t->stats);
@@ -1338,6 +1345,8 @@ extern "C" midsx_status midsx_gpu_tallies_reset(midsx_tallies_h t, void* stream)
     CUDA_TRY(cudaMemsetAsync(t->stats, 0, kStCount * sizeof(unsigned long long), s));
     if (t->acc_words) CUDA_TRY(cudaMemsetAsync(t->acc, 0, t->acc_words * 8, s));
     if (t->dose) CUDA_TRY(cudaMemsetAsync(t->dose, 0, t->n_voxels * t->dose_stride * 8, s));
+    if (t->batch) CUDA_TRY(cudaMemsetAsync(t->batch, 0, t->n_voxels * 16, s));
+    t->batches_closed = 0;
     t->precision = -1;
     return MIDSX_OK;
 }
@@ -1555,6 +1564,34 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
                  : launch_typed<double, false>(tables, P, cfg, block, s);
 }
 
+// Closes batch k (1-based) of a MIDSX_DOSE_BATCHES tally: per voxel the sum accumulated
+// since the last close (record word 0 minus word 3, exact in the fixed-point form) enters the
+// running mean and sum of squared deviations (Welford's update), and word 3 takes the sum.
+__global__ void batch_fold_kernel(unsigned long long* rec, size_t n, int mixed, double* mv, int k) {
+    const double inv_k = 1.0 / double(k);
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        unsigned long long* r = rec + i * 4;
+        const unsigned long long cur = r[0], last = r[3];
+        const double d = mixed ? double((long long)(cur - last)) / kFxEnergy
+                               : __longlong_as_double((long long)cur) - __longlong_as_double((long long)last);
+        r[3] = cur;
+        const double mean = mv[2 * i], delta = d - mean, m = mean + delta * inv_k;
+        mv[2 * i] = m;
+        mv[2 * i + 1] += delta * (d - m);
+    }
+}
+
+// Launches the fold of the next batch of `t` on `s`.
+midsx_status close_batch(midsx_gpu_tallies* t, int sm_count, cudaStream_t s) {
+    if (!t->batch || t->n_voxels == 0) return MIDSX_OK;
+    ++t->batches_closed;
+    batch_fold_kernel<<<std::max(1, sm_count) * 8, 256, 0, s>>>(t->dose, t->n_voxels,
+                                                               t->precision == MIDSX_PREC_MIXED, t->batch,
+                                                               t->batches_closed);
+    CUDA_TRY(cudaGetLastError());
+    return MIDSX_OK;
+}
+
 midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_source_h source,
                         midsx_tallies_h tallies, const midsx_run_config* cfg, void* stream,
                         double* trace = nullptr) {
@@ -1583,6 +1620,11 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
         set_last_error("the mixed form's fixed-point tallies take source energies up to 262144 eV");
         return MIDSX_INVALID_ARG;
     }
+    if (cfg->variance_batches < 0 || cfg->variance_batches > 1024 ||
+        (cfg->variance_batches > 1 && !tallies->batch)) {
+        set_last_error("variance_batches: 0..1024, and 2 or more only into MIDSX_DOSE_BATCHES tallies");
+        return MIDSX_INVALID_ARG;
+    }
     if (cfg->n_histories == 0) return MIDSX_OK;
     // a per-history trace runs the lane-parking kernel, which has reference tracking only:
     // refuse other tracking before anything is built for it (macro cells allocate)
@@ -1607,9 +1649,31 @@ midsx_status launch_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_so
     P.total = cfg->n_histories;
     P.trace = trace;
     P.spectra = tallies->spectra;
-    midsx_status st = launch_kernel(tables, P, *cfg, false, stream);
-    if (st == MIDSX_OK) tallies->precision = cfg->precision;
-    return st;
+    if (!tallies->batch) {
+        midsx_status st = launch_kernel(tables, P, *cfg, false, stream);
+        if (st == MIDSX_OK) tallies->precision = cfg->precision;
+        return st;
+    }
+    // MIDSX_DOSE_BATCHES: one launch per batch over consecutive history ranges, each closed
+    const uint64_t nb = uint64_t(std::max(1, cfg->variance_batches));
+    if (nb > cfg->n_histories) {
+        set_last_error("variance_batches exceeds the run's histories");
+        return MIDSX_INVALID_ARG;
+    }
+    uint64_t first = cfg->first_history;
+    for (uint64_t b = 0; b < nb; ++b) {
+        const uint64_t n = cfg->n_histories / nb + (b < cfg->n_histories % nb ? 1 : 0);
+        P.job0.first = first;
+        P.job0.n = n;
+        P.total = n;
+        first += n;
+        midsx_status st = launch_kernel(tables, P, *cfg, false, stream);
+        if (st != MIDSX_OK) return st;
+        tallies->precision = cfg->precision;
+        st = close_batch(tallies, tables->sm_count, static_cast<cudaStream_t>(stream));
+        if (st != MIDSX_OK) return st;
+    }
+    return MIDSX_OK;
 }
 
 double fx_signed(unsigned long long v, double scale) { return double((long long)v) / scale; }
@@ -1694,6 +1758,42 @@ extern "C" midsx_status midsx_gpu_fetch_dose(midsx_tallies_h t, double* sum, dou
         if (outs[k]) good = cuda_ok(cudaMemcpyAsync(outs[k], dev[k], n * 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
     for (int k = 0; k < 3; ++k)
         if (dev[k]) cudaFreeAsync(dev[k], s);
+    if (!good) return MIDSX_CUDA_ERROR;
+    return wait_stream(stream);
+}
+
+namespace {
+__global__ void batch_variance_kernel(const double* mv, size_t n, double scale, double* var) {
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        var[i] = mv[2 * i + 1] * scale;
+}
+}  // namespace
+
+// B s^2 with s^2 = M2 / (B - 1), the Welford sum of squared deviations of the batch sums.
+extern "C" midsx_status midsx_gpu_fetch_dose_variance(midsx_tallies_h t, double* var, int32_t* n_batches,
+                                                      void* stream) {
+    if (!t || !var || !t->batch) {
+        set_last_error("midsx_gpu_fetch_dose_variance: tallies without MIDSX_DOSE_BATCHES");
+        return MIDSX_INVALID_ARG;
+    }
+    if (t->batches_closed < 2) {
+        set_last_error("midsx_gpu_fetch_dose_variance: fewer than two batches closed");
+        return MIDSX_INVALID_ARG;
+    }
+    const size_t n = t->n_voxels;
+    if (n_batches) *n_batches = t->batches_closed;
+    if (n == 0) return MIDSX_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double* dev = nullptr;
+    if (!cuda_ok(cudaMallocAsync(&dev, n * 8, s), "cudaMallocAsync")) return MIDSX_CUDA_ERROR;
+    const double B = double(t->batches_closed);
+    int sms = 0, device = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    batch_variance_kernel<<<std::max(1, sms) * 8, 256, 0, s>>>(t->batch, n, B / (B - 1.0), dev);
+    bool good = cuda_ok(cudaGetLastError(), "batch_variance_kernel") &&
+                cuda_ok(cudaMemcpyAsync(var, dev, n * 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    cudaFreeAsync(dev, s);
     if (!good) return MIDSX_CUDA_ERROR;
     return wait_stream(stream);
 }
@@ -2324,6 +2424,8 @@ midsx_status tallies_create_async(midsx_phantom_h phantom, const midsx_tally_spe
     if (!t->host_specs.empty()) t->specs = reinterpret_cast<DevTally*>(base + off);
     off += t->host_specs.size() * sizeof(DevTally);
     if (t->dose_stride) t->dose = reinterpret_cast<unsigned long long*>(base + off);
+    off += t->n_voxels * size_t(t->dose_stride) * 8;
+    if (dose_mode == MIDSX_DOSE_BATCHES) t->batch = reinterpret_cast<double*>(base + off);
     for (auto& d : t->host_specs) d.acc = t->acc + reinterpret_cast<size_t>(d.acc);
     bool ok = cuda_ok(cudaMemsetAsync(base, 0, bytes, s), "cudaMemsetAsync");
     // the records are copied from the handle's own host vector, which outlives the copy

@@ -22,7 +22,7 @@ MACRO_CELL = 8  # voxels per macro-cell edge (MIDSX_MACRO_CELL)
 DIR_BEAM, DIR_ISOTROPIC, DIR_RECTANGLE, DIR_DISC = range(4)
 SPEC_MONO, SPEC_POLY = 0, 1
 TALLY_DISC, TALLY_RECT, TALLY_BINNED_RECT, TALLY_AACUBOID = 1, 2, 3, 4
-DOSE_OFF, DOSE_SUM, DOSE_FULL = 0, 1, 2
+DOSE_OFF, DOSE_SUM, DOSE_FULL, DOSE_BATCHES = 0, 1, 2, 3
 
 D3 = C.c_double * 3
 I3 = C.c_int32 * 3
@@ -86,7 +86,7 @@ class RunConfig(C.Structure):
                 ("max_compton_trials", C.c_int32), ("block_size", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("regroup", C.c_int32), ("chunk", C.c_int32),
                 ("scheduler", C.c_int32), ("tracking", C.c_int32), ("steps_per_pass", C.c_int32),
-                ("seed", C.c_uint64),
+                ("variance_batches", C.c_int32), ("reserved", C.c_int32), ("seed", C.c_uint64),
                 ("first_history", C.c_uint64), ("n_histories", C.c_uint64)]
 
 
@@ -170,6 +170,7 @@ _SIGNATURES = {
     "midsx_gpu_run": (C.c_int, [VP, VP, VP, VP, C.POINTER(RunConfig), VP]),
     "midsx_gpu_fetch_stats": (C.c_int, [VP, C.POINTER(RunStats), VP]),
     "midsx_gpu_fetch_dose": (C.c_int, [VP, PD, PD, PD, VP]),
+    "midsx_gpu_fetch_dose_variance": (C.c_int, [VP, PD, C.POINTER(C.c_int32), VP]),
     "midsx_gpu_fetch_scalar": (C.c_int, [VP, C.c_int32, PD, VP]),
     "midsx_gpu_fetch_binned": (C.c_int, [VP, C.c_int32, PD, PD, VP]),
     "midsx_gpu_fetch_spectrum": (C.c_int, [VP, C.c_int32, PD, PD, VP]),

@@ -222,3 +222,37 @@ def tables_like(t):
     TableBlob `t` (built by oracle/tables.py, not taken from `t`)."""
     host = getattr(t, "host", t)
     return tables.tables(tuple(int(m) for m in host.ids), float(host.e_max))
+
+
+def run_batches(blob, batches, n, seed=1, first=0, rng=RNG_PHILOX, **kw):
+    """run() split into `batches` runs over consecutive history ranges (with the mt19937
+    generator, each batch seeded on its own), summed; out["dose"]["var"] is the batch-method
+    variance of each voxel's sum, B / (B - 1) sum_b (S_b - S / B)^2 - the estimator of the
+    device's MIDSX_DOSE_BATCHES tallies, batch for batch on the same Philox streams."""
+    B = int(batches)
+    if B < 2 or B > n:
+        raise ValueError("2 <= batches <= n")
+    out, sums, start = None, [], int(first)
+    for b in range(B):
+        nb = n // B + (1 if b < n % B else 0)
+        r = run(blob, n=nb, seed=seed if rng == RNG_PHILOX else seed * 1009 + b, first=start, rng=rng, **kw)
+        start += nb
+        if "dose" in r:
+            sums.append(np.array(r["dose"]["sum"], dtype=np.float64))
+        out = r if out is None else _add_results(out, r)
+    if sums:
+        S = np.stack(sums)
+        out["dose"]["var"] = B / (B - 1) * ((S - S.mean(axis=0)) ** 2).sum(axis=0)
+        out["dose"]["batches"] = B
+    return out
+
+
+def _add_results(a, b):
+    """Sum of two run() results (counts, sums and arrays; run times added)."""
+    if isinstance(a, dict):
+        return {k: _add_results(a[k], b[k]) for k in a}
+    if isinstance(a, (list, tuple)):
+        return type(a)(_add_results(x, y) for x, y in zip(a, b))
+    if a is None:
+        return None
+    return a + b

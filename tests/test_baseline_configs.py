@@ -17,14 +17,20 @@
   (surface_quantity.cpp:49-63 classes).  No history reaches the step cap.
 
 The oracle runs with its own tables (oracle/tables.py restates the reference's table
-construction), so a table-build error of the product would show here as well.
+construction), so a table-build error of the product would show here as well.  Voxel
+z-scores divide by the batch-method variance of each run's sum (16 batches on both sides,
+MIDSX_DOSE_BATCHES on the device, oracle.run_batches on the CPU), not by the reference's
+per-deposit sigma (src/MIDSX/Core/quantity.cpp:37-45).
 """
 import numpy as np
 import pytest
 
 import midsx_gb300 as M
 import oracle
+from midsx_gb300 import native as N
 from midsx_gb300 import scenes
+
+BATCHES = 16
 
 pytestmark = pytest.mark.gpu
 
@@ -46,7 +52,8 @@ def assert_chi(z, beyond=0.01, label=""):
 
 
 def dose_var(d):
-    return d["var"] if "var" in d else d["sumsq"]
+    assert d.get("batches") == BATCHES
+    return d["var"]
 
 
 def z_bins(e_a, c_a, e_b, c_b, min_count=100):
@@ -68,6 +75,7 @@ def rebin(img, k):
 def cube():
     sc = scenes.water_cube()  # 100^3 at 1 mm, 100 x 100 bins
     assert sc.ids.shape == (100, 100, 100) and sc.specs[0]["nu"] == 100
+    sc.dose_mode = N.DOSE_BATCHES
     objs = sc.build()
     blob = oracle.tables_for(sc)
     return sc, objs, blob
@@ -77,11 +85,11 @@ def test_water_cube_fp64_equals_oracle_on_same_streams(cube):
     sc, (tables, ph, src, tl), blob = cube
     n = 1_000_000
     tl.reset()
-    M.run(tables, ph, src, tl, n, seed=1, precision="fp64")
+    M.run(tables, ph, src, tl, n, seed=1, precision="fp64", variance_batches=BATCHES)
     st = tl.stats()
     d = tl.dose()
     be, bc = tl.binned(0)
-    o = oracle.run(blob, n=n, seed=1, **sc.oracle_kwargs())
+    o = oracle.run_batches(blob, BATCHES, n=n, seed=1, **sc.oracle_kwargs())
     so = o["stats"]
     assert st["histories"] == so["histories"] == n
     assert st["step_cap_hits"] == so["step_cap_hits"] == 0
@@ -94,6 +102,9 @@ def test_water_cube_fp64_equals_oracle_on_same_streams(cube):
     g, c = d["sum"].ravel(), o["dose"]["sum"].ravel()
     same = np.abs(g - c) <= 1e-9 * np.maximum(1.0, np.abs(c))
     assert same.mean() > 0.999, same.mean()
+    # the same batches on the same streams: the batch variances agree as the sums do
+    vg, vc = d["var"].ravel(), o["dose"]["var"].ravel()
+    assert np.mean(np.abs(vg - vc) <= 1e-6 * np.maximum(vc, 1e-30) + 1e-9 * vc.max()) > 0.999
     oe, oc = o["binned"][0]
     assert np.mean(bc == oc) > 0.999
     assert be.sum() == pytest.approx(oe.sum(), rel=1e-4)
@@ -104,11 +115,11 @@ def test_water_cube_against_independent_oracle_full_size(cube, precision):
     sc, (tables, ph, src, tl), blob = cube
     n = 1_000_000
     tl.reset()
-    M.run(tables, ph, src, tl, n, seed=1, precision=precision)
+    M.run(tables, ph, src, tl, n, seed=1, precision=precision, variance_batches=BATCHES)
     st = tl.stats()
     d = tl.dose()
     be, bc = tl.binned(0)
-    o = oracle.run(blob, n=n, seed=1, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
+    o = oracle.run_batches(blob, BATCHES, n=n, seed=1, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
     so = o["stats"]
     assert st["step_cap_hits"] == 0
     bal = st["deposited_grid"] + st["deposited_background"] + st["escaped_energy"]
@@ -129,13 +140,14 @@ def test_water_cube_against_independent_oracle_full_size(cube, precision):
 def test_cone_beam_full_phantom_against_independent_oracle(precision):
     sc = scenes.cone_beam_dose(n_histories=1)
     assert sc.ids.shape == (128, 256, 256)
+    sc.dose_mode = N.DOSE_BATCHES
     tables, ph, src, tl = sc.build()
     blob = oracle.tables_for(sc)
     n = 2_000_000
-    M.run(tables, ph, src, tl, n, seed=41, precision=precision)
+    M.run(tables, ph, src, tl, n, seed=41, precision=precision, variance_batches=BATCHES)
     st = tl.stats()
     d = tl.dose()
-    o = oracle.run(blob, n=n, seed=42, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
+    o = oracle.run_batches(blob, BATCHES, n=n, seed=42, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
     so = o["stats"]
     assert st["step_cap_hits"] == 0 and so["step_cap_hits"] == 0
     assert abs(st["deposited_grid"] - so["deposited_grid"]) / so["deposited_grid"] < 0.005
@@ -229,7 +241,7 @@ def test_isotropic_source_against_oracle():
     sc = scenes.Scene("isotropic_point_in_water", [scenes.AIR, scenes.WATER], (20, 20, 20), (0.1, 0.1, 0.1),
                       (8, 8, 8), ids, scenes.AIR, source,
                       [dict(kind="cuboid", min=(8, 8, 8), max=(10, 12, 12)),
-                       dict(kind="disc", center=(10, 10, 19), normal=(0, 0, 1), radius=5.0)], 2, 1, 100e3)
+                       dict(kind="disc", center=(10, 10, 19), normal=(0, 0, 1), radius=5.0)], N.DOSE_BATCHES, 1, 100e3)
     tables, ph, src, tl = sc.build()
     blob = oracle.tables_for(sc)
     n = 200_000
@@ -238,9 +250,9 @@ def test_isotropic_source_against_oracle():
     assert np.mean(np.abs(g - o) <= 1e-9 * np.maximum(1.0, o)) > 0.999
     for precision in ("fp64", "mixed"):
         tl.reset()
-        M.run(tables, ph, src, tl, n, seed=3, precision=precision)
+        M.run(tables, ph, src, tl, n, seed=3, precision=precision, variance_batches=BATCHES)
         d = tl.dose()
-        oo = oracle.run(blob, n=n, seed=4, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
+        oo = oracle.run_batches(blob, BATCHES, n=n, seed=4, rng=oracle.RNG_MT19937, **sc.oracle_kwargs())
         for t in (0, 1):
             gs, os_ = tl.scalar(t), oo["scalar"][t]
             # photons counted (all classes): Poisson, within 4 sigma
@@ -253,3 +265,36 @@ def test_isotropic_source_against_oracle():
             assert abs(a - b) < 4 * np.sqrt(va + vb) + 1e-9 * abs(b), (precision, t, a, b)
         assert_chi(z_voxels(d["sum"].ravel(), dose_var(d).ravel(), oo["dose"]["sum"].ravel(),
                             dose_var(oo["dose"]).ravel()), beyond=0.015, label=precision)
+
+
+# -------------------------------------------------------- batch-method variance ---
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_batch_variance_equals_the_batches_computed_on_the_host(precision):
+    """MIDSX_DOSE_BATCHES against the same batches run one by one into DOSE_FULL tallies,
+    their sums differenced on the host: the same B / (B - 1) sum_b (S_b - S / B)^2 (exact
+    integer batch sums in the mixed form; FP64 atomics round in thread order)."""
+    sc = scenes.water_cube(n=30, bins=4)
+    tables, ph, src, _ = sc.build()
+    tb = M.Tallies(ph, (), N.DOSE_BATCHES)
+    tf = M.Tallies(ph, (), N.DOSE_FULL)
+    n, B = 120_000, 8
+    M.run(tables, ph, src, tb, n, seed=9, first=5, precision=precision, variance_batches=B)
+    got = tb.dose()
+    assert got["batches"] == B
+    prev, batch_sums, first = 0.0, [], 5
+    for b in range(B):
+        M.run(tables, ph, src, tf, n // B, seed=9, first=first, precision=precision)
+        first += n // B
+        cur = tf.dose()["sum"].ravel().copy()
+        batch_sums.append(cur - prev)
+        prev = cur
+    S = np.stack(batch_sums)
+    expect = B / (B - 1) * ((S - S.mean(axis=0)) ** 2).sum(axis=0)
+    np.testing.assert_allclose(got["sum"].ravel(), prev, rtol=1e-12 if precision == "fp64" else 0)
+    tol = 1e-12 if precision == "mixed" else 1e-8
+    np.testing.assert_allclose(got["var"].ravel(), expect, rtol=tol, atol=tol * expect.max())
+    # a second run adds one batch (each run closes at least one); a reset clears them
+    M.run(tables, ph, src, tb, 1000, seed=10, precision=precision)
+    assert tb.dose()["batches"] == B + 1
+    tb.reset()
+    assert "var" not in tb.dose()
