@@ -35,7 +35,8 @@ class OracleResult(C.Structure):
                 ("binned_energy", PD), ("binned_count", PD), ("history_deposit", PD),
                 ("stats", N.RunStats), ("run_time", C.c_double),
                 ("spectrum_count", PD), ("spectrum_cosine", PD), ("raw_spec", C.c_int32), ("reserved", C.c_int32),
-                ("raw_cap", C.c_int64), ("raw_energy", PD), ("raw_cosine", PD), ("raw_n", C.c_int64)]
+                ("raw_cap", C.c_int64), ("raw_energy", PD), ("raw_cosine", PD), ("raw_n", C.c_int64),
+                ("dose_var_hist", PD)]
 
 
 _lib = None
@@ -99,7 +100,7 @@ def run(blob, domain, spacing, origin, ids, background_id, source, specs=(), n=1
     keep = {}
     nvox = ids.size
     if dose:
-        for k in ("dose_sum", "dose_sumsq", "dose_count"):
+        for k in ("dose_sum", "dose_sumsq", "dose_count", "dose_var_hist"):
             keep[k] = np.zeros(nvox)
             setattr(res, k, N.dptr(keep[k]))
     n_scalar = len(specs)
@@ -152,6 +153,7 @@ def run(blob, domain, spacing, origin, ids, background_id, source, specs=(), n=1
 
     if dose:
         out["dose"] = {"sum": shaped(keep["dose_sum"]), "sumsq": shaped(keep["dose_sumsq"]),
+                       "var_hist": shaped(keep["dose_var_hist"]),
                        "count": shaped(keep["dose_count"])}
     out["scalar"] = [keep["scalar"][i * N.SCALAR_SLOTS:(i + 1) * N.SCALAR_SLOTS] for i in range(n_scalar)]
     binned, off = [], 0
@@ -224,11 +226,13 @@ def tables_like(t):
     return tables.tables(tuple(int(m) for m in host.ids), float(host.e_max))
 
 
-def run_batches(blob, batches, n, seed=1, first=0, rng=RNG_PHILOX, **kw):
+def run_batches(blob, batches, n, seed=1, first=0, rng=RNG_PHILOX, reduce=None, **kw):
     """run() split into `batches` runs over consecutive history ranges (with the mt19937
     generator, each batch seeded on its own), summed; out["dose"]["var"] is the batch-method
     variance of each voxel's sum, B / (B - 1) sum_b (S_b - S / B)^2 - the estimator of the
-    device's MIDSX_DOSE_BATCHES tallies, batch for batch on the same Philox streams."""
+    device's MIDSX_DOSE_BATCHES tallies, batch for batch on the same Philox streams.  With
+    `reduce` (a function of a batch's dose-sum array, e.g. block sums) the variance is that of
+    the reduced sums, and out["dose"]["batch_sums"] holds the B reduced batch sums."""
     B = int(batches)
     if B < 2 or B > n:
         raise ValueError("2 <= batches <= n")
@@ -238,12 +242,15 @@ def run_batches(blob, batches, n, seed=1, first=0, rng=RNG_PHILOX, **kw):
         r = run(blob, n=nb, seed=seed if rng == RNG_PHILOX else seed * 1009 + b, first=start, rng=rng, **kw)
         start += nb
         if "dose" in r:
-            sums.append(np.array(r["dose"]["sum"], dtype=np.float64))
+            a = np.array(r["dose"]["sum"], dtype=np.float64)
+            sums.append(reduce(a) if reduce else a)
         out = r if out is None else _add_results(out, r)
     if sums:
         S = np.stack(sums)
         out["dose"]["var"] = B / (B - 1) * ((S - S.mean(axis=0)) ** 2).sum(axis=0)
         out["dose"]["batches"] = B
+        if reduce:
+            out["dose"]["batch_sums"] = S
     return out
 
 

@@ -713,6 +713,7 @@ struct PhysicsEngine {
 struct ThreadState {
     std::vector<TallyReplica> tallies;
     std::vector<TempVoxelData> voxel_data;
+    std::vector<TempVoxelData> history_voxel;  // per history and voxel: all its deposits there
     Counters cnt;
     Generator gen;
 };
@@ -745,6 +746,11 @@ typedef struct oracle_result {
     double* raw_energy;
     double* raw_cosine;
     int64_t raw_n;
+    /* per-history variance of each voxel's dose sum, or NULL: N / (N - 1) * (sum_h x_h^2 -
+     * S^2 / N), x_h the energy history h deposited in the voxel (all its deposits there
+     * together), S the voxel's sum - the estimator the reference's event-based sigma
+     * (src/MIDSX/Core/quantity.cpp:37-45) is not */
+    double* dose_var_hist;
 } oracle_result;
 
 }  // extern "C"
@@ -948,6 +954,7 @@ int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size
                 }
             }
             double hist_dep = 0;
+            const size_t hv0 = st.history_voxel.size();
             for (auto& d : tx) {
                 if (d.energy_deposited != 0.0) {
                     if (d.voxel >= 0) {
@@ -955,6 +962,12 @@ int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size
                         st.cnt.dep_grid += d.energy_deposited;
                         hist_dep += d.energy_deposited;
                         st.cnt.words++;
+                        if (out->dose_var_hist) {  // this history's total in the voxel
+                            size_t k = hv0;
+                            while (k < st.history_voxel.size() && st.history_voxel[k].voxel != d.voxel) ++k;
+                            if (k == st.history_voxel.size()) st.history_voxel.push_back({d.voxel, 0.0});
+                            st.history_voxel[k].energy_deposited += d.energy_deposited;
+                        }
                     } else {
                         st.cnt.dep_bg += d.energy_deposited;
                     }
@@ -971,7 +984,7 @@ int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size
     }
     out->run_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     // merge replicas (getVolume/SurfaceQuantityContainers, addVoxelDataToComputationalDomain)
-    if (out->dose_sum || out->dose_sumsq || out->dose_count) {
+    if (out->dose_sum || out->dose_sumsq || out->dose_count || out->dose_var_hist) {
         std::vector<double> s(nvox, 0.0), s2(nvox, 0.0), c(nvox, 0.0);
         for (auto& st : states)
             for (auto& d : st.voxel_data) {
@@ -979,6 +992,14 @@ int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size
                 s2[size_t(d.voxel)] += d.energy_deposited * d.energy_deposited;
                 c[size_t(d.voxel)] += 1;
             }
+        if (out->dose_var_hist) {
+            std::vector<double> h2(nvox, 0.0);
+            for (auto& st : states)
+                for (auto& d : st.history_voxel) h2[size_t(d.voxel)] += d.energy_deposited * d.energy_deposited;
+            const double N = double(n);
+            for (size_t i = 0; i < nvox; ++i)
+                out->dose_var_hist[i] = N > 1 ? N / (N - 1) * std::max(0.0, h2[i] - s[i] * s[i] / N) : 0.0;
+        }
         if (out->dose_sum) std::memcpy(out->dose_sum, s.data(), nvox * 8);
         if (out->dose_sumsq) std::memcpy(out->dose_sumsq, s2.data(), nvox * 8);
         if (out->dose_count) std::memcpy(out->dose_count, c.data(), nvox * 8);
