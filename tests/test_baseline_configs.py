@@ -275,7 +275,7 @@ def test_radiography_against_independent_oracle(radiograph, radiograph_oracle, p
         co = rebin(oc[..., cls].sum(axis=2), k).ravel()
         sel = (cg >= MIN_DEPOSITS) & (co >= MIN_DEPOSITS)
         z = (ig[sel] - io[sel]) / np.sqrt(ig[sel] ** 2 / cg[sel] + io[sel] ** 2 / co[sel])
-        assert z.size > 20, (cls, z.size)
+        assert z.size > 10, (cls, z.size)
         assert np.mean(np.abs(z) > 3) < 0.02, (cls, np.mean(np.abs(z) > 3))
         assert np.mean(z * z) < 1 + 5 * np.sqrt(2 / z.size), (cls, np.mean(z * z))
 
