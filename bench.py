@@ -43,7 +43,10 @@ def parse():
     p.add_argument("--serving", type=int, default=1, help="run the serving leg (1/0)")
     p.add_argument("--serving-requests", type=int, default=120, help="requests at 200/s in the serving leg")
     p.add_argument("--radiography", type=int, default=1, help="run the radiography precision-ablation leg (1/0)")
-    p.add_argument("--radiography-histories", type=float, default=1e6, help="histories per precision (radiography)")
+    p.add_argument("--radiography-histories", type=float, default=1e6,
+                   help="histories per precision (radiography, reference tracking)")
+    p.add_argument("--radiography-macro-histories", type=float, default=1e8,
+                   help="histories per precision (radiography, macro-cell tracking)")
     p.add_argument("--radiography-only", action="store_true",
                    help="run the radiography precision-ablation leg alone and print its JSON (profiling)")
     return p.parse_args()
@@ -142,6 +145,16 @@ def job_rate(dist, world, steps, n_hist, total_s, device="cuda"):
     return world * steps * n_hist / total_s, total_s
 
 
+def rel_diff_stats(np, a, b, frac=0.01):
+    """|a - b| / b over the entries of b above frac x its maximum: p50, p99, max and the
+    count - the per-voxel (or per-bin) error of one precision against the other."""
+    a, b = np.asarray(a, dtype=np.float64).ravel(), np.asarray(b, dtype=np.float64).ravel()
+    sel = b > frac * b.max()
+    r = np.abs(a[sel] - b[sel]) / b[sel]
+    return {"entries": int(sel.sum()), "p50": float(np.percentile(r, 50)), "p99": float(np.percentile(r, 99)),
+            "max": float(r.max()), "total_rel_diff": float(abs(a.sum() - b.sum()) / b.sum())}
+
+
 def reference_arm(args, world, rank):
     """CPU restatement of the reference transport, all host threads, bounded samples."""
     if rank != 0:
@@ -237,7 +250,7 @@ def main():
     step_ms = [e[0].elapsed_time(e[2]) for e in evs]
     kern_ms = [e[1].elapsed_time(e[2]) for e in evs]
     value, total_s = job_rate(dist, world, args.steps, N_hist, sum(step_ms) / 1e3)
-    st = tl.stats()
+    st = tl.stats()  # raises MidsxError(STEP_CAP) if any history reached the step cap
     result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
               "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport / int64 fixed-point tallies",
@@ -250,7 +263,8 @@ def main():
               "clocks": clk, "gpu_launches": args.steps,
               "step_latency_ms": {"p50": statistics.median(step_ms), "p99": float(np.percentile(step_ms, 99))},
               "steps_per_history": st["steps"] / st["histories"],
-              "voxel_fetches_per_history": st["voxel_fetches"] / st["histories"]}
+              "voxel_fetches_per_history": st["voxel_fetches"] / st["histories"],
+              "step_cap_hits": st["step_cap_hits"]}
     if rank != 0:
         return
     if not args.quick:
@@ -263,22 +277,19 @@ def main():
         torch.cuda.synchronize()
         t64 = sum(e[1].elapsed_time(e[2]) for e in ev64) / 1e3
         plain = 2 * n64 / t64
-        # matched dose error: identical streams through both precisions
-        ncmp = min(N_hist, 2_000_000)
+        # error of the mixed form against the FP64 form on identical Philox streams: the
+        # per-voxel relative difference of the dose sums (voxels above 1 % of the maximum)
+        ncmp = min(N_hist, 4_000_000)
         doses = {}
         for p in ("fp64", "mixed"):
             tl.reset(sptr)
             M.run(tables, ph, src, tl, ncmp, seed=77, precision=p, stream=sptr)
-            doses[p] = tl.dose(sptr)
-        s64, s32 = doses["fp64"]["sum"].ravel(), doses["mixed"]["sum"].ravel()
-        q64, q32 = doses["fp64"]["sumsq"].ravel(), doses["mixed"]["sumsq"].ravel()
-        sel = s64 > 0.01 * s64.max()
-        z = (s32[sel] - s64[sel]) / np.sqrt(q32[sel] + q64[sel])
+            doses[p] = tl.dose(sptr)["sum"]
         result["plain_fp64"] = {"value": plain, "unit": UNIT, "histories_per_step": n64,
                                 "mixed_over_plain": value / world / plain}
-        result["matched_dose_error"] = {
-            "histories": ncmp, "total_dose_rel_diff": float(abs(s32.sum() - s64.sum()) / s64.sum()),
-            "voxels_compared": int(sel.sum()), "frac_voxels_beyond_3sigma": float(np.mean(np.abs(z) > 3))}
+        result["mixed_vs_fp64_identical_streams"] = dict(
+            histories=ncmp, **rel_diff_stats(np, doses["mixed"], doses["fp64"]))
+        result["batch_variance"] = batch_variance_leg(M, np, torch, sc, tables, ph, src, sptr, flush, N_hist)
         # end to end through the C ABI with host buffers (pinned), copies inside the timing
         ids_pinned = torch.from_numpy(sc.ids.ravel()).pin_memory()
         dose_pinned = torch.empty(ph.n_voxels, dtype=torch.float64).pin_memory()
@@ -346,6 +357,8 @@ def main():
         for mode in ("background_fast", "macro_cell"):
             result[mode + "_tracking"] = fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, N_hist,
                                                            mode)
+    if not args.quick:
+        result["water_cube_plain"] = water_cube_leg(args, np, torch)
     if not args.quick and args.radiography:
         result["radiography_precision_ablation"] = radiography_leg(args, np, torch)
     if not args.quick and args.batched:
@@ -374,7 +387,7 @@ def fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, n_hist, mo
         torch.cuda.synchronize()
         if i:
             times.append(ev[0].elapsed_time(ev[1]) / 1e3)
-    st = tl.stats()
+    st = tl.stats(allow_cap=True)
     ncmp = 2_000_000
     doses = {}
     for m in ("reference", mode):
@@ -388,6 +401,7 @@ def fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, n_hist, mo
     z = (s1[sel] - s2[sel]) / np.sqrt(q1[sel] + q2[sel])
     return {"value": n_hist / (sum(times) / len(times)), "unit": UNIT, "histories_per_step": n_hist,
             "steps_timed": len(times), "steps_per_history": st["steps"] / st["histories"],
+            "step_cap_hits": st["step_cap_hits"],
             "dose_vs_reference_tracking": {"histories": ncmp, "voxels_compared": int(sel.sum()),
                                            "frac_voxels_beyond_3sigma": float(np.mean(np.abs(z) > 3)),
                                            "total_rel_diff": float(abs(s1.sum() - s2.sum()) / s1.sum())}}
@@ -396,10 +410,12 @@ def fast_tracking_leg(M, np, torch, tables, ph, src, tl, sptr, flush, n_hist, mo
 def radiography_leg(args, np, torch):
     """Config 3, the precision ablation: the 512x512x256 radiography phantom at 0.5 mm (40
     ellipsoids and sixteen 2 mm lead spheres), 100 kVp, 512^2 detector of 1 mm bins at 100 cm
-    SID, primary and scattered fluence per bin - the mixed and the FP64 path on identical
-    Philox streams, on a bounded history count (the reference algorithm needs ~17.5k Woodcock
-    steps per history here: lead sets the global majorant along the whole 100 cm), plus the
-    opt-in background fast tracking."""
+    SID, primary and scattered fluence per bin.  The mixed and the FP64 path run on identical
+    Philox streams; the error of the mixed form is the per-bin relative difference of its
+    images against the FP64 images.  With the reference algorithm (global majorant: ~17.5k
+    Woodcock steps per history, lead sets it along the whole 100 cm) on a bounded history
+    count; with the opt-in macro-cell majorants on 1e8 histories in both precisions (the
+    config's 1e9 would take ~6 s mixed, ~1 min FP64)."""
     import midsx_gb300 as M
     from midsx_gb300 import scenes
     t0 = time.time()
@@ -418,39 +434,115 @@ def radiography_leg(args, np, torch):
         torch.cuda.synchronize()
         return ev[0].elapsed_time(ev[1]) / 1e3
 
+    def ablation(n, tracking, seed):
+        images, out = {}, {}
+        for precision in ("mixed", "fp64"):
+            dt = timed(n, precision, tracking, seed)
+            e, c = tl.binned(0, sptr)
+            images[precision] = e
+            st = tl.stats(sptr)  # raises if a history reached the step cap
+            out[precision] = {"value": n / dt, "unit": UNIT, "steps_per_history": st["steps"] / st["histories"],
+                              "step_cap_hits": st["step_cap_hits"]}
+        a, b = images["mixed"], images["fp64"]
+        err = {}
+        for name, cls in (("primary", [0]), ("scatter", [1, 2, 3])):
+            ia, ib = a[..., cls].sum(axis=2), b[..., cls].sum(axis=2)
+            err[name] = rel_diff_stats(np, ia, ib)
+            err[name]["bins_identical"] = float(np.mean(ia[ib > 0] == ib[ib > 0]))
+            k = 8  # 64 x 64 image of 8 x 8 bins
+            ra = ia.reshape(ia.shape[0] // k, k, ia.shape[1] // k, k).sum(axis=(1, 3))
+            rb = ib.reshape(ib.shape[0] // k, k, ib.shape[1] // k, k).sum(axis=(1, 3))
+            err[name + "_8x8_rebinned"] = rel_diff_stats(np, ra, rb)
+        return {"histories": n, "tracking": tracking, "mixed": out["mixed"], "fp64": out["fp64"],
+                "mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"],
+                "mixed_vs_fp64_identical_streams": err}, images["mixed"]
+
     n = int(args.radiography_histories)
     timed(n // 10, "mixed")  # warm-up
-    images, out = {}, {}
-    for precision in ("mixed", "fp64"):
-        dt = timed(n, precision)
-        e, c = tl.binned(0, sptr)
-        images[precision] = e
+    ref, ref_img = ablation(n, "reference", 5)
+    macro, macro_img = ablation(int(args.radiography_macro_histories), "macro_cell", 7)
+    # the opt-in modes against the reference algorithm (different streams: statistical)
+    prim_ref, scat_ref = ref_img[..., 0].sum(), ref_img[..., 1:].sum()
+    nm = int(args.radiography_macro_histories)
+    macro["primary_per_history_rel_diff_vs_reference"] = float(
+        abs(macro_img[..., 0].sum() / nm - prim_ref / n) / (prim_ref / n))
+    macro["scatter_per_history_rel_diff_vs_reference"] = float(
+        abs(macro_img[..., 1:].sum() / nm - scat_ref / n) / (scat_ref / n))
+    dt = timed(n, "mixed", tracking="background_fast", seed=6)
+    st = tl.stats(sptr)
+    e, _ = tl.binned(0, sptr)
+    bg = {"histories": n, "value": n / dt, "unit": UNIT, "steps_per_history": st["steps"] / st["histories"],
+          "step_cap_hits": st["step_cap_hits"],
+          "primary_total_rel_diff_vs_reference": float(abs(e[..., 0].sum() - prim_ref) / prim_ref),
+          "scatter_total_rel_diff_vs_reference": float(abs(e[..., 1:].sum() - scat_ref) / scat_ref)}
+    return {"workload": sc.name + " (512^2 detector at 100 cm SID, 16 Pb spheres)",
+            "reference_tracking": ref, "macro_cell_tracking": macro, "background_fast_tracking": bg}
+
+
+def water_cube_leg(args, np, torch):
+    """Config 1, the plain-method drop-in: 100^3 water voxels at 1 mm in a 20 cm air box, 60 keV
+    pencil beam, 100 x 100 exit-plane bins, 1e6 histories per run (seed 1), per-voxel dose.
+    The FP64 plain kernel and the mixed kernel (five timed runs each, device events), the
+    mixed form's per-voxel and per-bin error against FP64 on identical streams, and the CPU
+    oracle on the same 1e6 histories (all host threads)."""
+    import midsx_gb300 as M
+    import oracle
+    from midsx_gb300 import scenes
+    sc = scenes.water_cube()
+    tables, ph, src, tl = sc.build()
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    n = 1_000_000
+    out, dose, bins = {}, {}, {}
+    for precision in ("fp64", "mixed"):
+        tl.reset(sptr)
+        M.run(tables, ph, src, tl, n, seed=1, precision=precision, stream=sptr)  # warm-up, and the error data
         st = tl.stats(sptr)
-        out[precision] = {"value": n / dt, "unit": UNIT, "steps_per_history": st["steps"] / st["histories"]}
-    # identical streams: primary (class 0) and scattered (classes 1-3) energy per bin
-    a, b = images["mixed"], images["fp64"]
-    prim_a, prim_b = a[..., 0].ravel(), b[..., 0].ravel()
-    scat_a, scat_b = a[..., 1:].sum(axis=2).ravel(), b[..., 1:].sum(axis=2).ravel()
-    hit = prim_b > 0
-    rel = np.abs(prim_a[hit] - prim_b[hit]) / prim_b[hit]
-    opt_in = {}
-    for mode, seed in (("background_fast", 6), ("macro_cell", 7)):
-        dt = timed(n, "mixed", tracking=mode, seed=seed)
-        st = tl.stats(sptr)
-        e, c = tl.binned(0, sptr)
-        p = e[..., 0].ravel()
-        opt_in[mode] = {"value": n / dt, "unit": UNIT, "steps_per_history": st["steps"] / st["histories"],
-                        "primary_total_rel_diff_vs_reference": float(abs(p.sum() - prim_a.sum()) / prim_a.sum()),
-                        "scatter_total_rel_diff_vs_reference":
-                            float(abs(e[..., 1:].sum() - scat_a.sum()) / scat_a.sum())}
-    return {"workload": sc.name + " (512^2 detector at 100 cm SID, 16 Pb spheres)", "histories": n,
-            "mixed": out["mixed"], "fp64": out["fp64"], "mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"],
-            "identical_streams": {
-                "primary_total_rel_diff": float(abs(prim_a.sum() - prim_b.sum()) / prim_b.sum()),
-                "scatter_total_rel_diff": float(abs(scat_a.sum() - scat_b.sum()) / scat_b.sum()),
-                "primary_bins_identical": float(np.mean(prim_a[hit] == prim_b[hit])) if hit.any() else None,
-                "primary_bins_rel_diff_p99": float(np.percentile(rel, 99)) if hit.any() else None},
-            "opt_in_tracking": opt_in}
+        dose[precision] = tl.dose(sptr)["sum"]
+        bins[precision] = tl.binned(0, sptr)[0].sum(axis=2)
+        times = []
+        for i in range(5):
+            tl.reset(sptr)
+            ev[0].record(stream)
+            M.run(tables, ph, src, tl, n, seed=1, first=(i + 1) * n, precision=precision, stream=sptr)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            times.append(ev[0].elapsed_time(ev[1]) / 1e3)
+        out[precision] = {"value": n / statistics.mean(times), "unit": UNIT, "ms_per_run": 1e3 * statistics.mean(times),
+                          "steps_per_history": st["steps"] / st["histories"], "step_cap_hits": st["step_cap_hits"]}
+    threads = os.cpu_count() or 1
+    r = oracle.run(oracle.tables_for(sc), n=n, seed=1, rng=oracle.RNG_MT19937, threads=threads, **sc.oracle_kwargs())
+    return {"workload": sc.name + " (100^3 at 1 mm, 100 x 100 exit-plane bins)", "histories": n,
+            "fp64": out["fp64"], "mixed": out["mixed"],
+            "cpu_oracle": {"value": n / r["run_time"], "unit": UNIT, "cores": threads},
+            "mixed_vs_fp64_identical_streams": {"dose_voxels": rel_diff_stats(np, dose["mixed"], dose["fp64"]),
+                                                "exit_plane_bins": rel_diff_stats(np, bins["mixed"], bins["fp64"])}}
+
+
+def batch_variance_leg(M, np, torch, sc, tables, ph, src, sptr, flush, n_hist):
+    """The headline workload with the batch-method dose variance (MIDSX_DOSE_BATCHES): one
+    step split into 10 and into 100 batches, against the same step without batches - the
+    cost of a history-based variance on top of the reference's per-deposit sums."""
+    from midsx_gb300 import native as N
+    stream = torch.cuda.current_stream()
+    tb = M.Tallies(ph, sc.specs, N.DOSE_BATCHES)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    out = {}
+    for B in (1, 10, 100):
+        times = []
+        for i in range(3):
+            flush.zero_()
+            tb.reset(sptr)
+            ev[0].record(stream)
+            M.run(tables, ph, src, tb, n_hist, seed=1, first=(200 + i) * n_hist, precision="mixed", stream=sptr,
+                  variance_batches=B)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            times.append(ev[0].elapsed_time(ev[1]) / 1e3)
+        out["batches_%d" % B] = {"value": n_hist / statistics.mean(times), "unit": UNIT}
+    tb.close()
+    return out
 
 
 def batched_leg(args, torch):
