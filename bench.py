@@ -621,6 +621,7 @@ def serving_leg(args):
     def brief(d, lam):
         s = d["server"]
         return {"rate_req_per_s": lam, "requests": d["requests"], "failed": d["failed"],
+                "step_cap_hits": d["step_cap_hits"], "compton_cap_hits": d["compton_cap_hits"],
                 "histories_per_s": d["histories_per_s"], "offered_histories_per_s": d["offered_histories_per_s"],
                 "latency_ms": d["latency_ms"], "server_latency_ms": d["server_latency_ms"],
                 "by_class": d["by_class"], "launches": s["launches"], "max_active": s["max_active_seen"],

@@ -52,7 +52,8 @@ class Mix:
         """Results of a done request in host memory (dose arrays or detector images)."""
         sc = self.templates[req["cls"]][req["template"]]
         tl = self.server.tallies(rid)
-        out = {"stats": tl.stats()}
+        # a history that reached a cap is counted and reported by drive(), not raised here
+        out = {"stats": tl.stats(allow_cap=True)}
         if sc.dose_mode:
             out["dose"] = tl.dose()
         for i, spec in enumerate(sc.specs):
@@ -73,6 +74,7 @@ def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3
     t_host = [None] * n
     infos = [None] * n
     results = [None] * n if keep else None
+    caps = [None] * n
     errors = []
     submitted = threading.Semaphore(0)
 
@@ -91,6 +93,8 @@ def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3
                 if info["state"] in (N.REQ_DONE, N.REQ_FAILED):
                     if info["state"] == N.REQ_DONE:
                         res = mix.read(rids[i], requests[i])
+                        st = res["stats"]
+                        caps[i] = (st["step_cap_hits"], st["compton_cap_hits"])
                         if keep:
                             results[i] = res
                     else:
@@ -124,8 +128,12 @@ def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3
     for c in sorted({r["cls"] for r in requests}):
         li = [t_host[i] - t_arr[i] for i in range(n) if requests[i]["cls"] == c and t_host[i] is not None]
         by_cls[c] = {"requests": len(li), "p50_ms": 1e3 * float(np.median(li)) if li else None,
-                     "p99_ms": 1e3 * float(np.percentile(li, 99)) if li else None}
+                     "p99_ms": 1e3 * float(np.percentile(li, 99)) if li else None,
+                     "step_cap_hits": int(sum(caps[i][0] for i in range(n) if requests[i]["cls"] == c and caps[i])),
+                     "compton_cap_hits": int(sum(caps[i][1] for i in range(n)
+                                                 if requests[i]["cls"] == c and caps[i]))}
     out = {"requests": n, "failed": len(errors), "histories": hist, "span_s": span,
+           "step_cap_hits": int(sum(c[0] for c in caps if c)), "compton_cap_hits": int(sum(c[1] for c in caps if c)),
            "histories_per_s": hist / span, "offered_histories_per_s": hist / max(requests[-1]["t"], 1e-9),
            "latency_ms": {"p50": 1e3 * float(np.median(lat)), "p99": 1e3 * float(np.percentile(lat, 99)),
                           "max": 1e3 * float(lat.max())},
