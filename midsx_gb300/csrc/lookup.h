@@ -128,6 +128,12 @@ MIDSX_HD R lin_eval_at_log(const R* lx, const R* ly, int n, int idx, R lq) {
     if (idx >= n) return exp10_(ly[n - 1]);
     R x1 = lx[idx - 1], x2 = lx[idx];
     R y1 = ly[idx - 1], y2 = ly[idx];
+    if constexpr (sizeof(R) == 4) {
+        // Two nodes of the FP64 grid closer than FP32 resolves in log10 (merged grids hold node
+        // pairs a few meV apart) have one float log10 energy: a zero-width interval, whose slope
+        // would be infinite.  The value there is the left node's.
+        if (!(x2 > x1)) return exp10_(y1);
+    }
     R slope = (y2 - y1) / (x2 - x1);
     return exp10_(y1 + slope * (lq - x1));
 }
@@ -164,7 +170,10 @@ MIDSX_HD R spline_eval_at_log(const R* knot_u, const R* ctrl, int degree, int sp
         right[j] = knot_u[span + j] - u;
         R saved = R(0);
         for (int r = 0; r < j; ++r) {
-            R temp = N[r] / (right[r + 1] + left[j - r]);
+            // knots that coincide in the working precision: 0/0 is taken as 0, the usual
+            // convention of the recursion (the basis function over an empty span is zero)
+            const R den = right[r + 1] + left[j - r];
+            R temp = den != R(0) ? N[r] / den : R(0);
             N[r] = saved + right[r + 1] * temp;
             saved = left[j - r] * temp;
         }
