@@ -312,6 +312,7 @@ struct DevMaterial {
 struct DevTables {
     const double* d;     // FP64 data (blob layout)
     const float* f;      // FP32 copy, same offsets
+    const float* fs;     // FP32 LogLogLinear slopes at the ly offsets (lin_eval_slope_at_log)
     const int* rows;     // RITA row starts
     const int* bk;       // bucket tables of every searched node array
     BucketSpec bs[2][2];  // [kind][0 = FP64 query, 1 = FP32 query]
@@ -357,7 +358,13 @@ MIDSX_HD int lin_index_bk(const DevTables& t, const DevLin& L, R q) {
 template <typename R>
 MIDSX_HD R lin_lookup(const DevTables& t, const DevLin& L, R q) {
     const R* D = tab<R>(t);
-    return lin_eval_at(D + L.lx, D + L.ly, L.n, lin_index_bk<R>(t, L, q), q);
+    const int idx = lin_index_bk<R>(t, L, q);
+    if constexpr (sizeof(R) == 4) {
+        if (idx == 0 || idx >= L.n) return lin_eval_slope_at_log(D + L.lx, D + L.ly, t.fs + L.ly, L.n, idx, R(0));
+        return lin_eval_slope_at_log(D + L.lx, D + L.ly, t.fs + L.ly, L.n, idx, log10_(q));
+    } else {
+        return lin_eval_at(D + L.lx, D + L.ly, L.n, idx, q);
+    }
 }
 
 // Knot span with the bucketed search (same result as spline_span).
@@ -412,7 +419,10 @@ MIDSX_HD R lin_lookup_key(const DevTables& t, const DevLin& L, const EnergyKey<R
         const int* st = buckets<R>(t, L.bk_d, L.bk_f);
         idx = upper_index(x, st[k.b], st[k.b + 1], k.q);
     }
-    return lin_eval_at_log(D + L.lx, D + L.ly, L.n, idx, k.lq);
+    if constexpr (sizeof(R) == 4)
+        return lin_eval_slope_at_log(D + L.lx, D + L.ly, t.fs + L.ly, L.n, idx, k.lq);
+    else
+        return lin_eval_at_log(D + L.lx, D + L.ly, L.n, idx, k.lq);
 }
 
 // spline_lookup with a precomputed key: same span, same value.

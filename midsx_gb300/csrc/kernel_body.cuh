@@ -112,20 +112,6 @@ __device__ __forceinline__ unsigned long long fx_stat(float e) {
     return (unsigned long long)__float2uint_rn(e * float(kFxStat));
 }
 
-// A majorant that is not finite (a table that is broken at this energy) would hold the photon
-// where it is, taking zero-length steps until the step cap.  The history is counted as a
-// table-range error instead (the fetches then report MIDSX_TABLE_RANGE) and leaves the
-// domain at its next step, its energy counted as escaped.
-template <typename R>
-__device__ __forceinline__ void check_majorant(R& mu_max, R& inv_mu_max, V3<R>& pos, unsigned long long* st) {
-    if (!(mu_max < R(INFINITY))) {
-        stat_add(st, kStRangeErr, 1);
-        pos = {R(-1), R(-1), R(-1)};
-        mu_max = R(1);
-        inv_mu_max = R(1);
-    }
-}
-
 // Distance along the ray p + t d (t >= 0) to the closed box [lo, lo + ext], +inf if the ray
 // misses it (slab method) or meets it for no more than `tol` (grazing it, or leaving it from
 // a point within tol of its far side); 0 if p is inside.
@@ -584,7 +570,6 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
                     hist_dep = R(0);
                     mu_max = refresh_energy<R>(P, E, thr, mucache, stride);
                     inv_mu_max = R(1) / mu_max;
-                    check_majorant<R>(mu_max, inv_mu_max, pos, sj);
                     alive = true;
                 }
             } else {
@@ -663,7 +648,6 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
                         } else if (energy_changed) {
                             mu_max = refresh_energy<R>(P, E, thr, mucache, stride);
                             inv_mu_max = R(1) / mu_max;
-                            check_majorant<R>(mu_max, inv_mu_max, pos, st);
                         }
                     }
                 }

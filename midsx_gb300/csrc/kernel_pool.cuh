@@ -528,7 +528,6 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         if (need_refresh) {
             mu_max = refresh_energy<R>(P, E, S.thr + sl, S.mu + sl, ns);
             inv_mu_max = R(1) / mu_max;
-            check_majorant<R>(mu_max, inv_mu_max, pos, s_stats + job * kStCount);
         }
         // survivors and new histories go to the ready list
         {

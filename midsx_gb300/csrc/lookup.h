@@ -128,14 +128,20 @@ MIDSX_HD R lin_eval_at_log(const R* lx, const R* ly, int n, int idx, R lq) {
     if (idx >= n) return exp10_(ly[n - 1]);
     R x1 = lx[idx - 1], x2 = lx[idx];
     R y1 = ly[idx - 1], y2 = ly[idx];
-    if constexpr (sizeof(R) == 4) {
-        // Two nodes of the FP64 grid closer than FP32 resolves in log10 (merged grids hold node
-        // pairs a few meV apart) have one float log10 energy: a zero-width interval, whose slope
-        // would be infinite.  The value there is the left node's.
-        if (!(x2 > x1)) return exp10_(y1);
-    }
     R slope = (y2 - y1) / (x2 - x1);
     return exp10_(y1 + slope * (lq - x1));
+}
+
+// LogLogLinear value on interval idx with the interval's slope given (sl[idx] for the interval
+// [idx - 1, idx]), for the FP32 tables: their slopes are computed in FP64 on the host and
+// rounded once.  Grid nodes closer than FP32 resolves in log10 (merged grids hold node pairs a
+// few meV apart) share one float log10 energy, a zero-width interval whose slope recomputed in
+// FP32 would be infinite; the stored slope stays finite, and no division is left on the device.
+template <typename R>
+MIDSX_HD R lin_eval_slope_at_log(const R* lx, const R* ly, const R* sl, int n, int idx, R lq) {
+    if (idx == 0) return exp10_(ly[0]);
+    if (idx >= n) return exp10_(ly[n - 1]);
+    return exp10_(ly[idx - 1] + sl[idx] * (lq - lx[idx - 1]));
 }
 
 template <typename R>
@@ -170,10 +176,7 @@ MIDSX_HD R spline_eval_at_log(const R* knot_u, const R* ctrl, int degree, int sp
         right[j] = knot_u[span + j] - u;
         R saved = R(0);
         for (int r = 0; r < j; ++r) {
-            // knots that coincide in the working precision: 0/0 is taken as 0, the usual
-            // convention of the recursion (the basis function over an empty span is zero)
-            const R den = right[r + 1] + left[j - r];
-            R temp = den != R(0) ? N[r] / den : R(0);
+            R temp = N[r] / (right[r + 1] + left[j - r]);
             N[r] = saved + right[r + 1] * temp;
             saved = left[j - r] * temp;
         }

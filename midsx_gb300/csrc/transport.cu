@@ -545,6 +545,7 @@ struct midsx_gpu_tables {
     DevTables T;
     double* d = nullptr;
     float* f = nullptr;
+    float* fs = nullptr;  // FP32 LogLogLinear slopes (computed in FP64), same offsets as d
     int* rows = nullptr;
     int* bk = nullptr;
     int32_t ids[MIDSX_MAX_MATERIALS];
@@ -759,6 +760,27 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
     f64_to_f32_kernel<<<unsigned((nd + 255) / 256), 256>>>(h->d, h->f, nd);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaDeviceSynchronize());
+    // FP32 spline knots: interior knots of the FP64 vector that round to the knot before them
+    // (parameters of grid energies a few meV apart) would give the FP32 basis recursion a
+    // zero-width span and 0/0; each is raised to the next float above its predecessor, so the
+    // FP32 knot vector increases wherever the FP64 one does (a shift of a few ulps)
+    for (int m = 0; m < blob->n_materials; ++m) {
+        for (const midsx_spline_table* sp : {&blob->mat[m].coh, &blob->mat[m].incoh}) {
+            const int nk = sp->n_ctrl + sp->degree + 1;
+            const double* kd = blob->data + sp->knot_u;
+            std::vector<float> kf(static_cast<size_t>(nk));
+            bool changed = false;
+            for (int i = 0; i < nk; ++i) {
+                kf[size_t(i)] = float(kd[i]);
+                if (i > 0 && kd[i] > kd[i - 1] && !(kf[size_t(i)] > kf[size_t(i) - 1])) {
+                    kf[size_t(i)] = std::nextafter(kf[size_t(i) - 1], 2.0f);
+                    changed = true;
+                }
+            }
+            if (changed)
+                CUDA_TRY(cudaMemcpy(h->f + sp->knot_u, kf.data(), kf.size() * sizeof(float), cudaMemcpyHostToDevice));
+        }
+    }
     DevTables& T = h->T;
     T.d = h->d;
     T.f = h->f;
@@ -789,6 +811,31 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
         d.rita.n_energy = s.rita.n_energy;
         h->ids[m] = s.id;
     }
+    // FP32 slopes of every LogLogLinear table: (ly[i] - ly[i-1]) / (lx[i] - lx[i-1]) in FP64,
+    // rounded once (0 where two nodes share a log10 energy even in FP64)
+    {
+        std::vector<float> slopes(nd, 0.0f);
+        auto add = [&](const midsx_lin_table& L) {
+            const double* lx = blob->data + L.lx;
+            const double* ly = blob->data + L.ly;
+            for (int32_t i = 1; i < L.n; ++i) {
+                const double dx = lx[i] - lx[i - 1];
+                const double v = dx != 0.0 ? (ly[i] - ly[i - 1]) / dx : 0.0;
+                slopes[size_t(L.ly + i)] = std::isfinite(v) ? float(v) : 0.0f;
+            }
+        };
+        add(blob->majorant);
+        for (int m = 0; m < blob->n_materials; ++m) {
+            const midsx_material_table& s = blob->mat[m];
+            add(s.total);
+            add(s.photo);
+            add(s.sfunc);
+            add(s.ffactor);
+        }
+        if (!cuda_ok(cudaMalloc(&h->fs, nd * sizeof(float)), "cudaMalloc")) return MIDSX_OOM;
+        CUDA_TRY(cudaMemcpy(h->fs, slopes.data(), nd * sizeof(float), cudaMemcpyHostToDevice));
+        T.fs = h->fs;
+    }
     // bucket tables for every searched node array, FP64 and FP32 queries
     BucketBuilder bb;
     const double* D = blob->data;
@@ -815,6 +862,7 @@ extern "C" midsx_status midsx_gpu_tables_destroy(midsx_tables_h t) {
     if (!t) return MIDSX_INVALID_ARG;
     cudaFree(t->d);
     cudaFree(t->f);
+    cudaFree(t->fs);
     cudaFree(t->rows);
     cudaFree(t->bk);
     delete t;

@@ -338,3 +338,31 @@ def test_error_statuses():
     assert e.value.status == N.INVALID_ARG
     with pytest.raises(N.MidsxError):
         M.run(tables, ph, src, tl, 10, seed=1, precision="fp64")  # tallies hold mixed results
+
+
+def test_fp32_lookups_finite_on_grid_nodes_closer_than_float_resolution():
+    """Merged energy grids hold node pairs a few meV apart whose log10 energies round to one
+    float: in FP32 such an interval has zero width.  A majorant recomputing its slope there in
+    FP32 was infinite, and the photon took zero-length steps until the step cap (one history in
+    ~5e8 of the cone-beam workload).  The FP32 tables carry slopes computed in FP64: free paths
+    sampled at those nodes are finite and equal the FP64 ones on the same streams, and that
+    history now ends after a normal number of steps."""
+    sc = scenes.cone_beam_dose(n_histories=1)
+    tables, ph, src, tl = sc.build()
+    blob = tables.host
+    mj = blob.blob.majorant
+    x, lx = blob.array(mj.x, mj.n), blob.array(mj.lx, mj.n)
+    fx = lx.astype(np.float32)
+    bad = np.nonzero((fx[1:] <= fx[:-1]) & (lx[1:] > lx[:-1]) & np.isfinite(lx[:-1]))[0]
+    e = x[bad][(x[bad] > 1e3) & (x[bad] < 8e4)]
+    assert e.size > 20
+    for E in e[:: max(1, e.size // 40)]:
+        E32 = float(np.float32(E))
+        s32 = M.sample(tables, "freepath", 0, E32, 64, seed=5, precision="mixed")
+        s64 = M.sample(tables, "freepath", 0, E32, 64, seed=5, precision="fp64")
+        assert np.all(np.isfinite(s32)) and np.all(s32 > 0), E
+        np.testing.assert_allclose(s32, s64, rtol=2e-4, atol=1e-5 * s64.mean())
+    tl.reset()
+    M.run(tables, ph, src, tl, 1, seed=1, first=20200762447, precision="mixed")
+    st = tl.stats()
+    assert st["step_cap_hits"] == 0 and st["steps"] < 1000
