@@ -361,7 +361,11 @@ typedef struct midsx_run_config {
                                     the default, fixed at compile time. */
     int32_t variance_batches;    /* MIDSX_DOSE_BATCHES tallies: batches this run is split into
                                     (0 or 1: the run is one batch); at most 1024 */
-    int32_t reserved;
+    int32_t pass_repeats;        /* batched photon-pool launches: passes repeated without the
+                                    pool's list bookkeeping while fewer than 16 lanes of a warp
+                                    wait, 1..16 (0 = tuned default: 8 for the FP32 form with
+                                    reference tracking, else 1).  Single runs use the default,
+                                    fixed at compile time. */
     uint64_t seed;
     uint64_t first_history;      /* history ids [first, first + n) select Philox streams */
     uint64_t n_histories;
@@ -453,7 +457,8 @@ midsx_status midsx_gpu_batch_run(midsx_batch_h b, const midsx_run_config* cfg, v
  * `stream`; midsx_gpu_batch_replay launches it.  Replays advance the epoch like runs. */
 midsx_status midsx_gpu_batch_capture(midsx_batch_h b, const midsx_run_config* cfg, void* stream);
 midsx_status midsx_gpu_batch_replay(midsx_batch_h b, void* stream);
-/* Times candidate launch shapes (scheduler, block size, blocks per SM, regroup threshold,
+/* Times candidate launch shapes (scheduler, block size, blocks per SM, regroup threshold, steps per
+ * pass and pass repeats of the photon pool,
  * histories per fetch) on `trial_histories` histories spread over the jobs in proportion to
  * their sizes, returns the fastest in *best (precision as given) and its histories/s; the
  * trial runs leave the jobs' tallies reset and the epoch unchanged.  Synchronous. */

@@ -386,8 +386,10 @@ TRACKING = {"reference": N.TRACK_REFERENCE, "background_fast": N.TRACK_BACKGROUN
 
 
 def run_config(n, seed, first=0, precision="mixed", block=0, per_sm=0, max_steps=0, max_trials=0, regroup=0,
-               chunk=0, scheduler="default", tracking="reference", steps_per_pass=0, variance_batches=0):
+               chunk=0, scheduler="default", tracking="reference", steps_per_pass=0, variance_batches=0,
+               pass_repeats=0):
     c = N.RunConfig()
+    c.pass_repeats = int(pass_repeats)
     c.variance_batches = int(variance_batches)
     c.steps_per_pass = int(steps_per_pass)
     c.tracking = TRACKING[tracking] if isinstance(tracking, str) else int(tracking)
@@ -472,7 +474,7 @@ class Batch:
         N.check(N.load().midsx_gpu_batch_autotune(self.handle, PRECISIONS[precision], int(trial), C.byref(best),
                                                   C.byref(rate), stream), "midsx_gpu_batch_autotune")
         launch = dict(block=best.block_size, per_sm=best.blocks_per_sm, regroup=best.regroup, chunk=best.chunk,
-                      scheduler=best.scheduler, steps_per_pass=best.steps_per_pass)
+                      scheduler=best.scheduler, steps_per_pass=best.steps_per_pass, pass_repeats=best.pass_repeats)
         return launch, rate.value
 
     def close(self):

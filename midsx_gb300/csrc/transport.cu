@@ -153,6 +153,7 @@ struct RunParams {
     double* trace;  // optional (single job): energy deposited in grid voxels per history
     int spectra;    // some tally of the launch keeps an incident-energy spectrum
     int steps_per_pass;  // photon pool: Woodcock steps per pass of the warp loop
+    int pass_repeats;    // photon pool, batched: passes repeated between list bookkeeping
     int server;          // launched by the request server (its own steps_per_pass default)
     uint32_t round_keys[20];  // single-job launch: Philox key schedule of job0.seed
     Geo<float> geo_f;         // single-job launch: job0's geometry in either precision,
@@ -167,6 +168,11 @@ __device__ __forceinline__ const Geo<double>& job0_geo(const RunParams& P, doubl
 // batch (3, 4 and 6 were slower than 1).  The FP64 form (-2.3 % with 2), the opt-in modes
 // whose steps are long (a background flight, a cell walk; -8 to -9 % with 2) and the request
 // server's short mixed launches (-10 % histories/s, +12 % p99 latency with 2) keep one.
+// Batched launches: passes repeated between the pool's list bookkeeping (pass_repeats in
+// kernel_pool.cuh); single-job launches fix it at compile time.
+inline int default_pass_repeats(int precision, int tracking, bool server) {
+    return precision == MIDSX_PREC_MIXED && tracking == MIDSX_TRACK_REFERENCE && !server ? 8 : 1;
+}
 inline int default_steps_per_pass(int precision, int tracking, bool server) {
     return precision == MIDSX_PREC_MIXED && tracking == MIDSX_TRACK_REFERENCE && !server ? 2 : 1;
 }
@@ -1574,6 +1580,8 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
     }
     P.steps_per_pass = cfg.steps_per_pass > 0 ? cfg.steps_per_pass
                                                : default_steps_per_pass(cfg.precision, cfg.tracking, P.server != 0);
+    P.pass_repeats = cfg.pass_repeats > 0 ? std::min(cfg.pass_repeats, 16)
+                                          : default_pass_repeats(cfg.precision, cfg.tracking, P.server != 0);
     // cfg.max_steps = 0: the cap the caller derived from the jobs' geometry (P.max_steps)
     if (cfg.max_steps > 0) P.max_steps = cfg.max_steps;
     if (P.max_steps <= 0) P.max_steps = 100000;
@@ -2309,13 +2317,15 @@ extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precis
         if (!spectra)
             for (int bs : {64, 128, 256})
                 for (int sp : {1, 2})
-                    for (int rg : {24, 28, 32}) {
-                        c.block_size = bs;
-                        c.blocks_per_sm = 0;
-                        c.steps_per_pass = sp;
-                        c.regroup = rg;
-                        cands.push_back(c);
-                    }
+                    for (int pr : {1, 8})
+                        for (int rg : {24, 28, 32}) {
+                            c.block_size = bs;
+                            c.blocks_per_sm = 0;
+                            c.steps_per_pass = sp;
+                            c.pass_repeats = pr;
+                            c.regroup = rg;
+                            cands.push_back(c);
+                        }
     }
     double best_r = -1;
     RunParams P;

@@ -86,7 +86,7 @@ class RunConfig(C.Structure):
                 ("max_compton_trials", C.c_int32), ("block_size", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("regroup", C.c_int32), ("chunk", C.c_int32),
                 ("scheduler", C.c_int32), ("tracking", C.c_int32), ("steps_per_pass", C.c_int32),
-                ("variance_batches", C.c_int32), ("reserved", C.c_int32), ("seed", C.c_uint64),
+                ("variance_batches", C.c_int32), ("pass_repeats", C.c_int32), ("seed", C.c_uint64),
                 ("first_history", C.c_uint64), ("n_histories", C.c_uint64)]
 
 
