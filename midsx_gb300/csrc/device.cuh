@@ -90,6 +90,34 @@ MIDSX_HD void philox_round_keys(uint64_t seed, uint32_t* rk) {
     }
 }
 
+// The same generator inlined, the key schedule added as it goes: the Woodcock step of batched
+// launches, whose jobs have keys of their own (an out-of-line call per step spills around it).
+MIDSX_HD Philox4 philox4x32_10_inl(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+    uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint32_t hi0, lo0, hi1, lo1;
+        mulhilo32(0xD2511F53u, x0, hi0, lo0);
+        mulhilo32(0xCD9E8D57u, x2, hi1, lo1);
+        uint32_t y0 = hi1 ^ x1 ^ k0;
+        uint32_t y2 = hi0 ^ x3 ^ k1;
+        x0 = y0;
+        x1 = lo1;
+        x2 = y2;
+        x3 = lo0;
+    }
+    Philox4 o;
+    o.v[0] = x0;
+    o.v[1] = x1;
+    o.v[2] = x2;
+    o.v[3] = x3;
+    return o;
+}
+
 MIDSX_HD Philox4 philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const uint32_t (&rk)[20]) {
     uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3;
 #pragma unroll
@@ -148,6 +176,16 @@ struct HistoryRng {
     MIDSX_HD void next_pair64(uint64_t& first, uint64_t& second) {
         uint32_t blk = (n + 1u) >> 1;
         Philox4 w = philox4x32_10(blk, h0, h1, 0u, k0, k1);
+        first = (uint64_t(w.v[0]) << 32) | w.v[1];
+        second = (uint64_t(w.v[2]) << 32) | w.v[3];
+        b0 = w.v[2];
+        b1 = w.v[3];
+        n = 2u * blk + 2u;
+    }
+    // next_pair64 with the block computed inline (the batched kernels' Woodcock step)
+    MIDSX_HD void next_pair64_inl(uint64_t& first, uint64_t& second) {
+        uint32_t blk = (n + 1u) >> 1;
+        Philox4 w = philox4x32_10_inl(blk, h0, h1, 0u, k0, k1);
         first = (uint64_t(w.v[0]) << 32) | w.v[1];
         second = (uint64_t(w.v[2]) << 32) | w.v[3];
         b0 = w.v[2];

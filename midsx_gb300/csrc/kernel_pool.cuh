@@ -65,11 +65,82 @@ struct PoolSlots {
 constexpr int kPoolRealWords = 12;  // R arrays per slot
 constexpr int kPoolIntWords = 8;    // uint32 arrays per slot
 
+// Batched launches (MULTI) run job-affine blocks: a block works on one job at a time and holds
+// only that job in shared memory - its record (DevJob), its geometry in the working
+// precision, its run statistics and the block's control words - about 1 KB.  Blocks start
+// spread over the jobs in proportion to their histories; a block whose job has no histories
+// left to hand out lets its warps finish their photons (drain), flushes the job's statistics
+// and moves to the job with the most histories left.  Steps and events then run as in a
+// single-job launch, 7 blocks of 128 threads per SM (every job's counters and geometry in
+// shared memory, ~16 KB for 64 jobs, held batched launches to 24 warps per SM), and the tails of
+// different jobs overlap.  Each job hands out its histories from a counter of its own.
+constexpr int kBlockCtlWords = 4;  // current job, its histories this launch, spare
+constexpr int kBlockKeyWords = 20;  // the job's Philox key schedule (philox_round_keys)
 template <typename R>
 __host__ __device__ inline size_t pool_head_bytes(int n_jobs, bool multi) {
-    size_t b = size_t(n_jobs) * kStCount * 8;
-    if (multi) b += size_t(n_jobs + 1) * 8 + size_t(n_jobs) * sizeof(Geo<R>);
+    (void)n_jobs;
+    size_t b = size_t(kStCount) * 8;
+    if (multi)
+        b += sizeof(DevJob) + ((sizeof(Geo<R>) + 15) & ~size_t(15)) + kBlockCtlWords * 8 + kBlockKeyWords * 4;
     return (b + 15) & ~size_t(15);
+}
+
+// The job a block works on: its record in shared memory (batched) or the launch's own job0.
+template <bool MULTI>
+__device__ __forceinline__ const DevJob& pick_job(const RunParams& P, const DevJob* s_job) {
+    if constexpr (MULTI)
+        return *s_job;
+    else
+        return P.job0;
+}
+template <bool MULTI, typename R>
+__device__ __forceinline__ const Geo<R>& pick_geo(const RunParams& P, const Geo<R>* s_geo) {
+    if constexpr (MULTI)
+        return *s_geo;
+    else
+        return job0_geo(P, R(0));
+}
+
+// Batched launches: the next job of a block (warp 0 decides, all lanes return it): the job
+// whose history range holds the block's share of the launch on its first call, else the job
+// with the most histories left to hand out; -1 when every job is handed out.
+__device__ __forceinline__ int next_block_job(const RunParams& P, bool first) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned long long total = P.prefix[P.n_jobs];
+    if (first) {
+        const unsigned long long target =
+            (unsigned long long)((double(blockIdx.x) + 0.5) * double(total) / double(gridDim.x));
+        int lo = 0, hi = P.n_jobs;  // last job with prefix <= target
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (P.prefix[mid] <= target) lo = mid;
+            else hi = mid;
+        }
+        const unsigned long long n = P.prefix[lo + 1] - P.prefix[lo];
+        const unsigned long long c = *reinterpret_cast<volatile const unsigned long long*>(P.job_counters + lo);
+        if (c < n) return lo;
+    }
+    unsigned long long best = 0;
+    int best_j = -1;
+    for (int j = int(lane); j < P.n_jobs; j += 32) {
+        const unsigned long long n = P.prefix[j + 1] - P.prefix[j];
+        const unsigned long long c = *reinterpret_cast<volatile const unsigned long long*>(P.job_counters + j);
+        const unsigned long long rem = c < n ? n - c : 0ull;
+        if (rem > best) {
+            best = rem;
+            best_j = j;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oj = __shfl_xor_sync(0xffffffffu, best_j, o);
+        if (ob > best || (ob == best && oj >= 0 && (best_j < 0 || oj < best_j))) {
+            best = ob;
+            best_j = oj;
+        }
+    }
+    return best_j;
 }
 
 // Shared-memory bytes of a pool launch: per-job counters, batch prefix and geometry, the
@@ -93,21 +164,23 @@ __host__ __device__ inline size_t pool_smem(int n_jobs, bool multi, int n_materi
 // reference tracking, the background fast path's code cost the reference path 8 %).  SPEC:
 // the launch keeps incident-energy spectra (a kernel of its own too: the spectrum code cost
 // tally-free launches 5 %).  Batched
-// launches take blocks of up to 256 threads: their per-job counters and geometry in shared
-// memory (~16 KB for 64 jobs) are then shared by twice the photon slots.  Single-job FP32
-// launches run 7 blocks of 128 threads per SM (72 registers, a few bytes spilled): +6.5 %
-// against 6 blocks of 80 registers on the cone-beam dose workload.
+// launches hold one job per block (job-affine blocks, above).  FP32 launches run 7 blocks of
+// 128 threads per SM (72 registers, a few bytes spilled): +6.5 % against 6 blocks of 80
+// registers on the cone-beam dose workload.
 template <typename R, bool MULTI, int TRACK, bool SPEC = false>
-__global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3 : 7) : (MULTI ? 2 : 4))
-    transport_pool_kernel(const RunParams P) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_kernel(const RunParams P) {
     constexpr bool MX = sizeof(R) == 4;
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int njobs = MULTI ? P.n_jobs : 1;
+    const int njobs = 1;  // the statistics in shared memory are those of the block's one job
     const int M = P.T.n_materials;
     unsigned long long* s_stats = reinterpret_cast<unsigned long long*>(smem_raw);
-    unsigned long long* s_prefix = s_stats + njobs * kStCount;
-    Geo<R>* s_geo = reinterpret_cast<Geo<R>*>(s_prefix + (MULTI ? njobs + 1 : 0));
+    // batched: the block's job record, its geometry and the block's control words
+    DevJob* s_job = reinterpret_cast<DevJob*>(s_stats + kStCount);
+    Geo<R>* s_geo = reinterpret_cast<Geo<R>*>(reinterpret_cast<unsigned char*>(s_job) + sizeof(DevJob));
+    long long* s_ctl = reinterpret_cast<long long*>(reinterpret_cast<unsigned char*>(s_geo) +
+                                                    ((sizeof(Geo<R>) + 15) & ~size_t(15)));
+    uint32_t(&s_rk)[kBlockKeyWords] = *reinterpret_cast<uint32_t(*)[kBlockKeyWords]>(s_ctl + kBlockCtlWords);
     const int nw = int(blockDim.x >> 5);
     const int ns = nw * kPoolSlots;
     PoolSlots<R> S;
@@ -133,30 +206,37 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
     unsigned long long* scratch = reinterpret_cast<unsigned long long*>(
                                       smem_raw + pool_scratch_offset<R>(njobs, MULTI, M, int(blockDim.x))) +
                                   (threadIdx.x >> 5) * 32;
-    for (int i = threadIdx.x; i < njobs * kStCount; i += blockDim.x) s_stats[i] = 0;
-    if (MULTI) {
-        for (int i = threadIdx.x; i <= njobs; i += blockDim.x) s_prefix[i] = P.prefix[i];
-        for (int i = threadIdx.x; i < njobs; i += blockDim.x) s_geo[i] = make_geo<R>(P.jobs[i].G);
-    }
+    if constexpr (!MULTI)
+        for (int i = threadIdx.x; i < kStCount; i += blockDim.x) s_stats[i] = 0;
     const unsigned lane = threadIdx.x & 31u;
     const int warp = int(threadIdx.x >> 5);
     const unsigned below = (1u << lane) - 1u;
     const int sbase = warp * kPoolSlots;
     uint8_t* rdy = stacks + warp * 2 * kPoolSlots;  // ready list: slots to step
     uint8_t* evq = rdy + kPoolSlots;               // event list: slots waiting for an event
-    // every slot starts as a history start
-    evq[lane] = uint8_t(lane);
-    evq[lane + 32] = uint8_t(lane + 32);
-    S.meta[sbase + lane] = pack_meta(0, 0, 0, 0, kKindStart);
-    S.meta[sbase + lane + 32] = pack_meta(0, 0, 0, 0, kKindStart);
-    __syncthreads();
-    const Geo<R>& g0 = job0_geo(P, R(0));
+    // every slot starts as a history start (a batched block again for each of its jobs)
+    auto init_pool = [&]() {
+        evq[lane] = uint8_t(lane);
+        evq[lane + 32] = uint8_t(lane + 32);
+        S.meta[sbase + lane] = pack_meta(0, 0, 0, 0, kKindStart);
+        S.meta[sbase + lane + 32] = pack_meta(0, 0, 0, 0, kKindStart);
+    };
+    if constexpr (!MULTI) {
+        init_pool();
+        __syncthreads();
+    }
+    const Geo<R>& g0 = pick_geo<MULTI, R>(P, s_geo);
+    const DevJob& J = pick_job<MULTI>(P, s_job);
     const unsigned long long epoch = P.epoch ? *P.epoch : 0ull;
     const int regroup = max(1, min(P.regroup, 32));
     constexpr bool fast_mode = TRACK != MIDSX_TRACK_REFERENCE;   // background flights
     constexpr bool macro_mode = TRACK == MIDSX_TRACK_MACRO_CELL;  // and macro-cell flights in grids
     int rdy_top = 0, ev_top = kPoolSlots;  // warp-uniform list sizes
-    bool exhausted = false;                // warp-uniform: every history of the launch handed out
+    bool exhausted = false;                // warp-uniform: every history of the job handed out
+    // batched: the block's job's history counter and its histories in this launch (a single
+    // job reads the launch's own from the kernel parameters)
+    unsigned long long* job_counter = nullptr;
+    unsigned long long job_total = 0;
 
     // the photon in this lane's registers
     int cur = -1;  // slot stepped by this lane
@@ -180,7 +260,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         n_coh = int((meta >> 16) & 0x7fu);
         n_incoh = int((meta >> 23) & 0x7fu);
         kind = meta >> 30;
-        const uint64_t seed = MULTI ? P.jobs[job].seed : P.job0.seed;
+        const uint64_t seed = J.seed;
         rng.k0 = uint32_t(seed);
         rng.k1 = uint32_t(seed >> 32);
         rng.h0 = S.h0[sl];
@@ -194,7 +274,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         words = S.words[sl];
         // fast tracking steers by the last lookup's region (-1: background, -2: not known)
         if constexpr (fast_mode) vox = int(S.vox[sl]);
-        ntal = MULTI ? P.jobs[job].n_tallies : P.job0.n_tallies;
+        ntal = J.n_tallies;
     };
     auto load_event = [&](int sl) {  // a parked photon: flight state plus its collision site
         load_flight(sl);
@@ -241,6 +321,40 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         stat_add(st, kStWords, words);
     };
 
+    // single job: one pass of the job loop; batched: one per job the block works on
+    bool first_job = true;
+    do {
+    if constexpr (MULTI) {
+        if (warp == 0) {
+            const int j = next_block_job(P, first_job);
+            if (lane == 0) {
+                s_ctl[0] = j;
+                s_ctl[1] = j >= 0 ? (long long)(P.prefix[j + 1] - P.prefix[j]) : 0;
+            }
+        }
+        __syncthreads();
+        const int j = int(s_ctl[0]);
+        if (j < 0) break;
+        // the job's record to shared memory, its geometry in the working precision
+        {
+            const unsigned* src = reinterpret_cast<const unsigned*>(P.jobs + j);
+            unsigned* dst = reinterpret_cast<unsigned*>(s_job);
+            for (int i = threadIdx.x; i < int(sizeof(DevJob) / 4); i += blockDim.x) dst[i] = src[i];
+        }
+        if (threadIdx.x == 0) {
+            *s_geo = make_geo<R>(P.jobs[j].G);
+            philox_round_keys(P.jobs[j].seed, s_rk);
+        }
+        job_counter = P.job_counters + j;
+        job_total = (unsigned long long)s_ctl[1];
+        for (int i = threadIdx.x; i < kStCount; i += blockDim.x) s_stats[i] = 0;
+        init_pool();
+        rdy_top = 0;
+        ev_top = kPoolSlots;
+        exhausted = false;
+        cur = -1;
+        __syncthreads();
+    }
     for (;;) {
         // lanes without a photon take one from the ready list
         {
@@ -263,7 +377,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
             bool segment = false;  // the step's segment goes to the tallies (escape or delta step)
             if (cur >= 0) {
                 // one Woodcock step: getFreePath, move, domain test, voxel fetch, isDeltaScatter
-                const Geo<R>& g = MULTI ? s_geo[job] : g0;
+                const Geo<R>& g = g0;
                 unsigned long long* st = s_stats + job * kStCount;
                 if (steps >= uint32_t(P.max_steps)) {
                     stat_add(st, kStStepCap, 1);
@@ -272,7 +386,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
                     ++steps;
                     uint64_t w1, w2;
                     if constexpr (MULTI)
-                        rng.next_pair64(w1, w2);
+                        rng.next_pair64_rk(w1, w2, s_rk);
                     else
                         rng.next_pair64_rk(w1, w2, P.round_keys);
                     // MIDSX_TRACK_BACKGROUND_FAST: a photon known to be in the background (vox == -1
@@ -293,7 +407,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
                             tau = -log_(to_uniform(w1, R(0)));
                         bool bg = vox == -1;
                         if (macro_mode && !bg) {
-                            fl = cell_flight<R, MX>(g, MULTI ? P.jobs[job].G : P.job0.G, S.mu + cur, ns, pos, dir, tau,
+                            fl = cell_flight<R, MX>(g, J.G, S.mu + cur, ns, pos, dir, tau,
                                                     s, mu_c, tau_rem);
                             bg = fl == 2;
                         }
@@ -365,7 +479,7 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
             // collisions below) measured 3 % slower on the cone-beam dose workload and 29 % slower
             // on the radiography workload.
             if (segment && ntal > 0)
-                score_tallies<R, MX, SPEC>(MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, dir, s, E,
+                score_tallies<R, MX, SPEC>(J.tallies, ntal, p0, dir, s, E,
                                      scatter_class(n_coh, n_incoh), 0, false, R(0), words);
         }  // pass
         }  // repeats
@@ -478,10 +592,9 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         }
         // the collisions' tallies and voxel dose, aggregated over the warp
         if (__any_sync(FULL, scored && ntal > 0))
-            score_tallies_warp<R, MX, SPEC>(scored && ntal > 0, MULTI ? P.jobs[job].tallies : P.job0.tallies, ntal, p0, d0,
+            score_tallies_warp<R, MX, SPEC>(scored && ntal > 0, J.tallies, ntal, p0, d0,
                                       s, E0, cls0, scatter_class(n_coh, n_incoh), true, dep, words, scratch);
         {
-            const DevJob& J = MULTI ? P.jobs[job] : P.job0;
             const bool dosed = scored && dep != R(0) && vox >= 0 && J.dose_stride != 0;
             if (dosed) ++words;
             warp_record<R, MX>(dosed ? kRecDose : kRecNone, dosed ? J.dose + size_t(vox) * J.dose_stride : nullptr,
@@ -494,40 +607,26 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         // new histories: one atomic per warp hands out the lanes' history indices
         const unsigned nm = __ballot_sync(FULL, need_start);
         if (nm) {
-            unsigned long long base = P.total;
+            const unsigned long long total = MULTI ? job_total : P.total;
+            unsigned long long base = total;
             if (!exhausted) {
                 const int leader = __ffs(nm) - 1;
-                if (int(lane) == leader) base = atomicAdd(P.counter, (unsigned long long)__popc(nm));
+                if (int(lane) == leader)
+                    base = atomicAdd(MULTI ? job_counter : P.counter, (unsigned long long)__popc(nm));
                 base = __shfl_sync(FULL, base, leader);
-                if (base + (unsigned long long)__popc(nm) >= P.total) exhausted = true;
+                if (base + (unsigned long long)__popc(nm) >= total) exhausted = true;
             }
             if (need_start) {
                 const unsigned long long gidx = base + (unsigned long long)__popc(nm & below);
-                if (gidx >= P.total) {
+                if (gidx >= total) {
                     sl = -1;  // nothing left to start: the slot stays empty
                 } else {
-                    uint64_t seed, hid;
-                    if (MULTI) {
-                        int lo = 0, hi = njobs;  // last job with prefix <= gidx
-                        while (hi - lo > 1) {
-                            const int mid = (lo + hi) >> 1;
-                            if (s_prefix[mid] <= gidx) lo = mid;
-                            else hi = mid;
-                        }
-                        job = lo;
-                        const DevJob& J = P.jobs[job];
-                        seed = J.seed;
-                        hid = J.first + epoch * J.n + (gidx - s_prefix[job]);
-                        ntal = J.n_tallies;
-                    } else {
-                        job = 0;
-                        seed = P.job0.seed;
-                        hid = P.job0.first + epoch * P.job0.n + gidx;
-                        ntal = P.job0.n_tallies;
-                    }
+                    job = 0;
+                    const uint64_t hid = J.first + epoch * J.n + gidx;
+                    ntal = J.n_tallies;
                     // PhotonSource::generatePhoton + a fresh per-history stream
-                    rng.init(seed, hid);
-                    sample_source<R>(MULTI ? P.jobs[job].S : P.job0.S, rng, pos, dir, E);
+                    rng.init(J.seed, hid);
+                    sample_source<R>(J.S, rng, pos, dir, E);
                     unsigned long long* sj = s_stats + job * kStCount;
                     stat_add(sj, kStHistories, 1);
                     stat_add(sj, kStSourceE, fx_stat(E));
@@ -557,13 +656,13 @@ __global__ void __launch_bounds__(MULTI ? 256 : 128, sizeof(R) == 4 ? (MULTI ? 3
         __syncwarp();
         if (cur >= 0) load_flight(cur);  // back to the photon this lane was stepping
     }
+    // the job's histories are done in this block (the warps drained their pools)
     __syncthreads();
-    for (int i = threadIdx.x; i < njobs * kStCount; i += blockDim.x) {
+    for (int i = threadIdx.x; i < kStCount; i += blockDim.x) {
         const unsigned long long v = s_stats[i];
-        if (v) {
-            const int j = i / kStCount;
-            unsigned long long* dst = MULTI ? P.jobs[j].stats : P.job0.stats;
-            atomicAdd(dst + (i - j * kStCount), v);
-        }
+        if (v) atomicAdd(J.stats + i, v);
     }
+    if constexpr (MULTI) __syncthreads();  // the record and statistics are read before the next job replaces them
+    first_job = false;
+    } while (MULTI);  // jobs
 }

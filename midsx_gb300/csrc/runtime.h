@@ -28,7 +28,8 @@ midsx_status pack_job(midsx_tables_h tables, midsx_phantom_h phantom, midsx_sour
                       void* dst, uint32_t* step_cap = nullptr);
 
 // One batched launch over n_jobs records at `dev_jobs` with history offsets `dev_prefix`
-// (n_jobs + 1 words, last = total) and a history counter `dev_counter` zeroed here, on `s`.
+// (n_jobs + 1 words, last = total) and history counters `dev_counter` (1 + n_jobs words: the
+// launch's and each job's) zeroed here, on `s`.
 // spectra: some job's tallies keep an incident-energy spectrum (tallies_spectra), which the
 // lane-parking kernel scores.  step_cap: the launch's default per-history step cap (the
 // largest of its jobs' pack_job caps), used when cfg.max_steps is 0.

@@ -491,7 +491,7 @@ extern "C" midsx_status midsx_server_create(midsx_tables_h tables, const midsx_s
                ok(cudaMallocHost(reinterpret_cast<void**>(&sl.host_prefix), (kMaxJobs + 1) * 8), "cudaMallocHost") &&
                ok(cudaMalloc(&sl.dev_jobs, kMaxJobs * rec), "cudaMalloc") &&
                ok(cudaMalloc(reinterpret_cast<void**>(&sl.dev_prefix), (kMaxJobs + 1) * 8), "cudaMalloc") &&
-               ok(cudaMalloc(reinterpret_cast<void**>(&sl.dev_counter), 8), "cudaMalloc");
+               ok(cudaMalloc(reinterpret_cast<void**>(&sl.dev_counter), 8 * (1 + MIDSX_MAX_BATCH_JOBS)), "cudaMalloc");
     }
     s->t0 = Clock::now();
     if (!good) {

@@ -144,6 +144,7 @@ struct RunParams {
     int n_jobs;
     const unsigned long long* prefix;       // batched launch: n_jobs + 1 history offsets (device)
     unsigned long long* counter;            // histories handed out so far (zeroed before launch)
+    unsigned long long* job_counters;       // batched photon pool: each job's own (counter + 1 ...)
     unsigned long long total;               // histories of this launch
     const unsigned long long* epoch;        // optional: history ids advance by n per epoch
     int max_steps, max_trials;
@@ -1589,10 +1590,10 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
     P.regroup = cfg.regroup > 0 ? std::min(cfg.regroup, 32) : (pool ? 32 : 24);
     P.chunk = cfg.chunk > 0 ? std::min(cfg.chunk, 64) : 1;
     const bool mixed = cfg.precision == MIDSX_PREC_MIXED;
-    const int max_block = pool && !multi ? 128 : 256;
+    const int max_block = pool ? 128 : 256;
     int block = cfg.block_size > 0 ? cfg.block_size : max_block;
     if (block > max_block || block % 32) {
-        set_last_error(max_block == 128 ? "block_size must be a multiple of 32 up to 128 (photon pool, one job)"
+        set_last_error(max_block == 128 ? "block_size must be a multiple of 32 up to 128 (photon pool)"
                                         : "block_size must be a multiple of 32 up to 256");
         return MIDSX_INVALID_ARG;
     }
@@ -1607,7 +1608,9 @@ midsx_status launch_kernel(midsx_tables_h tables, RunParams& P, const midsx_run_
         return MIDSX_INVALID_ARG;
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    CUDA_TRY(cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), s));
+    // the launch's history counter and, for batched launches, each job's (the words after it)
+    P.job_counters = multi ? P.counter + 1 : nullptr;
+    CUDA_TRY(cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long) * (multi ? 1 + size_t(P.n_jobs) : 1), s));
     if (pool) {
         if (mixed) return multi ? launch_pool<float, true>(tables, P, cfg, block, s)
                                 : launch_pool<float, false>(tables, P, cfg, block, s);
@@ -2113,7 +2116,7 @@ struct midsx_gpu_batch {
     std::vector<midsx_tallies_h> tallies;
     DevJob* jobs = nullptr;
     unsigned long long* prefix = nullptr;
-    unsigned long long* words = nullptr;  // [0] history counter, [1] epoch
+    unsigned long long* words = nullptr;  // [0] epoch, [1] history counter, [2 ...] the jobs' counters
     cudaGraphExec_t graph = nullptr;
     int graph_precision = -1;
     double max_energy = 0;
@@ -2127,9 +2130,9 @@ void batch_params(const midsx_gpu_batch* b, RunParams& P, const unsigned long lo
     P.jobs = b->jobs;
     P.n_jobs = b->n_jobs;
     P.prefix = prefix;
-    P.counter = b->words;
+    P.counter = b->words + 1;
     P.total = total;
-    P.epoch = b->words + 1;
+    P.epoch = b->words;
     for (auto* t : b->tallies) P.spectra |= t->spectra;
     for (const DevJob& j : b->host_jobs) P.max_steps = std::max(P.max_steps, int(j.step_cap));
 }
@@ -2159,7 +2162,7 @@ midsx_status batch_enqueue(midsx_gpu_batch* b, const midsx_run_config& cfg, cuda
     if (P.total == 0) return MIDSX_OK;
     midsx_status st = launch_kernel(b->tables, P, cfg, true, s);
     if (st != MIDSX_OK) return st;
-    advance_epoch_kernel<<<1, 1, 0, s>>>(b->words + 1);
+    advance_epoch_kernel<<<1, 1, 0, s>>>(b->words);
     CUDA_TRY(cudaGetLastError());
     return MIDSX_OK;
 }
@@ -2194,12 +2197,12 @@ extern "C" midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const mids
     }
     if (!cuda_ok(cudaMalloc(&b->jobs, n_jobs * sizeof(DevJob)), "cudaMalloc") ||
         !cuda_ok(cudaMalloc(&b->prefix, (n_jobs + 1) * sizeof(unsigned long long)), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&b->words, 2 * sizeof(unsigned long long)), "cudaMalloc"))
+        !cuda_ok(cudaMalloc(&b->words, (2 + kMaxBatchJobs) * sizeof(unsigned long long)), "cudaMalloc"))
         return MIDSX_OOM;
     CUDA_TRY(cudaMemcpy(b->jobs, b->host_jobs.data(), n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(b->prefix, b->host_prefix.data(), (n_jobs + 1) * sizeof(unsigned long long),
                         cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemset(b->words, 0, 2 * sizeof(unsigned long long)));
+    CUDA_TRY(cudaMemset(b->words, 0, (2 + kMaxBatchJobs) * sizeof(unsigned long long)));
     guard.release();
     *out = b;
     return MIDSX_OK;
@@ -2315,7 +2318,7 @@ extern "C" midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precis
         bool spectra = false;
         for (auto* t : b->tallies) spectra |= t->spectra;
         if (!spectra)
-            for (int bs : {64, 128, 256})
+            for (int bs : {64, 128})
                 for (int sp : {1, 2})
                     for (int pr : {1, 8})
                         for (int rg : {24, 28, 32}) {
