@@ -610,7 +610,30 @@ def serving_leg(args):
     warm = [dict(t=0.0, cls=c[0], template=0, n=200_000, seed=999 + k, first=0)
             for k, c in enumerate(scenes.SERVING_CLASSES)]
     serving.drive(mix, warm)
+    # the kernel rate of the mix: one request of each class run alone (midsx_gpu_run, device
+    # events), weighted by the classes' histories in the stream
+    import torch
+    import midsx_gb300 as M
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    class_rate = {}
+    for name, _, n in scenes.SERVING_CLASSES:
+        sc = tmpl[name][0]
+        t = mix.tables[tuple(sc.materials)]
+        ph = M.Phantom(t, sc.domain, sc.spacing, sc.origin, sc.ids, sc.background)
+        tl = M.Tallies(ph, sc.specs, sc.dose_mode)
+        src = M.Source(**sc.source)
+        M.run(t, ph, src, tl, min(n, 2_000_000), seed=5, precision="mixed")
+        tl.reset()
+        ev[0].record()
+        M.run(t, ph, src, tl, n, seed=6, precision="mixed")
+        ev[1].record()
+        torch.cuda.synchronize()
+        class_rate[name] = n / (ev[0].elapsed_time(ev[1]) / 1e3)
+        tl.close()
+        ph.close()
     reqs = scenes.serving_requests(rate=200.0, n_requests=args.serving_requests, seed=1)
+    mix_hist = {c: sum(r["n"] for r in reqs if r["cls"] == c) for c in class_rate}
+    kernel_rate = sum(mix_hist.values()) / sum(mix_hist[c] / class_rate[c] for c in class_rate)
     hot = serving.drive(mix, reqs)
     mean_h = hot["histories"] / hot["requests"]
     rate = max(1.0, 0.8 * hot["histories_per_s"] / mean_h)
@@ -629,6 +652,8 @@ def serving_leg(args):
 
     return {"workload": "poisson mix: 70% 64^3 dose 1e6, 25% 128^3 dose 1e7, 5% 256x256x128 radiography "
                         "256^2 detector 1e8 (mixed precision)",
+            "kernel_rate_of_the_mix": {"value": kernel_rate, "unit": UNIT, "per_class": class_rate,
+                                       "how": "one request of each class alone, weighted by the stream's histories"},
             "at_200_req_per_s": brief(hot, 200.0), "at_sustainable_rate": brief(calm, rate)}
 
 

@@ -476,9 +476,11 @@ midsx_status midsx_gpu_batch_autotune(midsx_batch_h b, int32_t precision, uint64
  *    admitted in arrival order when a job slot is free and its footprint (its tallies, plus
  *    its phantom when that is not resident) fits the HBM budget.
  *  - A scheduler thread keeps up to `launches_in_flight` batched launches queued on the GPU.
- *    Each launch gives every admitted request with histories left a share of
- *    `launch_histories` (equal shares, smaller requests take only what they need), so a
- *    request that arrives while launches run joins the next launch.
+ *    Each launch splits `launch_histories` among the admitted requests with histories left:
+ *    three quarters go to the requests with the fewest histories left, each taking all it
+ *    needs in turn (shortest remaining first), and the rest is shared equally by the others,
+ *    so a small request that arrives while large ones run finishes in its next launch and
+ *    large requests keep progressing.
  *  - History ids, not launch boundaries, select the Philox streams: a request's results equal
  *    those of a single midsx_gpu_run of the same phantom, source, tallies, seed and range -
  *    bit for bit in the mixed form, to FP64 rounding order in the FP64 form.

@@ -328,18 +328,35 @@ bool midsx_gpu_server::launch_locked(bool setup_pending) {
             if (r->r.precision == precision && phantoms[size_t(r->r.phantom)]->tables == tables &&
                 r->scheduled < r->r.n_histories && int(cand.size()) < kMaxJobs)
                 cand.push_back(r);
-        // equal shares of the launch; requests that need less than a share take only that
+        // Size-aware shares.  Three quarters of the launch go to the requests with the fewest
+        // histories left, each taking all it needs in turn (shortest remaining first: a small
+        // dose request arriving behind 1e8-history radiographs finishes in its first launch);
+        // the last quarter, and whatever the small requests left, is shared equally by the
+        // requests still short (those that need less than a share take only that), so large
+        // requests keep progressing under any load.  Equal shares alone gave a 1e6-history
+        // request ~70k histories per launch in a mix of 57 requests: ~14 launches to finish.
         std::vector<Request*> order(cand);
         std::sort(order.begin(), order.end(), [](const Request* a, const Request* b) {
-            return a->r.n_histories - a->scheduled < b->r.n_histories - b->scheduled;
+            const uint64_t ra = a->r.n_histories - a->scheduled, rb = b->r.n_histories - b->scheduled;
+            return ra < rb || (ra == rb && a->admit_seq < b->admit_seq);
         });
-        uint64_t budget_h = launch_histories;
         std::map<Request*, uint64_t> give;
-        for (size_t k = 0; k < order.size(); ++k) {
-            const uint64_t rem = order[k]->r.n_histories - order[k]->scheduled;
-            const uint64_t share = std::max<uint64_t>(1, budget_h / uint64_t(order.size() - k));
+        uint64_t first_h = launch_histories - launch_histories / 4;
+        for (Request* r : order) {
+            const uint64_t g = std::min(r->r.n_histories - r->scheduled, first_h);
+            if (g == 0) break;
+            give[r] = g;
+            first_h -= g;
+        }
+        uint64_t budget_h = launch_histories / 4 + first_h;
+        std::vector<Request*> rest;
+        for (Request* r : order)
+            if (r->r.n_histories - r->scheduled > give[r]) rest.push_back(r);
+        for (size_t k = 0; k < rest.size(); ++k) {
+            const uint64_t rem = rest[k]->r.n_histories - rest[k]->scheduled - give[rest[k]];
+            const uint64_t share = std::max<uint64_t>(1, budget_h / uint64_t(rest.size() - k));
             const uint64_t g = std::min(rem, share);
-            give[order[k]] = g;
+            give[rest[k]] += g;
             budget_h -= std::min(budget_h, g);
         }
         // job records in admission order
@@ -350,6 +367,7 @@ bool midsx_gpu_server::launch_locked(bool setup_pending) {
         uint32_t step_cap = 0;
         for (Request* r : cand) {
             const uint64_t n = give[r];
+            if (n == 0) continue;  // no histories in this launch (the budget went to others)
             uint32_t job_cap = 0;
             midsx_status ps = midsx::rt::pack_job(tables, phantoms[size_t(r->r.phantom)]->h, r->r.source, r->tallies,
                                                   r->r.seed, r->r.first_history + r->scheduled, n, precision,

@@ -127,7 +127,17 @@ def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3
     by_cls = {}
     for c in sorted({r["cls"] for r in requests}):
         li = [t_host[i] - t_arr[i] for i in range(n) if requests[i]["cls"] == c and t_host[i] is not None]
-        by_cls[c] = {"requests": len(li), "p50_ms": 1e3 * float(np.median(li)) if li else None,
+        # where the time went (medians, ms): admission wait, wait for the first launch, the
+        # launches until done, and the host side (submission, polling, reading the results)
+        idx = [i for i in range(n) if requests[i]["cls"] == c and infos[i] is not None and t_host[i] is not None]
+        parts = {}
+        if idx:
+            f = lambda a, b: 1e3 * float(np.median([infos[i][b] - infos[i][a] for i in idx]))  # noqa: E731
+            parts = {"admission_wait": f("t_submit", "t_admit"), "first_launch_wait": f("t_admit", "t_first_launch"),
+                     "running": f("t_first_launch", "t_done"),
+                     "host_side": 1e3 * float(np.median([t_host[i] - t_arr[i] - (infos[i]["t_done"] - infos[i]["t_submit"])
+                                                         for i in idx]))}
+        by_cls[c] = {"requests": len(li), "p50_ms": 1e3 * float(np.median(li)) if li else None, "median_parts_ms": parts,
                      "p99_ms": 1e3 * float(np.percentile(li, 99)) if li else None,
                      "step_cap_hits": int(sum(caps[i][0] for i in range(n) if requests[i]["cls"] == c and caps[i])),
                      "compton_cap_hits": int(sum(caps[i][1] for i in range(n)
