@@ -40,6 +40,16 @@ def parse():
     p.add_argument("--quick", action="store_true", help="skip the FP64, e2e, CPU, batched and serving legs")
     p.add_argument("--batched", type=int, default=1, help="run the 64-job batched leg (1/0)")
     p.add_argument("--batch-scale", type=float, default=1.0, help="history scale of the batched jobs")
+    p.add_argument("--batch-fp64-scale", type=float, default=0.1,
+                   help="further history scale of the jobs of the batched FP64/mixed pair")
+    p.add_argument("--batch-jobs", type=int, default=64, help="jobs of the batched leg")
+    p.add_argument("--batch-autotune", type=int, default=1,
+                   help="autotune the batched launch shape (1) or take the default shape (0)")
+    p.add_argument("--batch-pair", type=int, default=1, help="run the batched FP64/mixed pair (1/0)")
+    p.add_argument("--batched-only", action="store_true",
+                   help="run the batched leg alone and print its JSON (profiling)")
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                   help="precision of the timed transport steps (fp64: the plain drop-in form, for profiling)")
     p.add_argument("--serving", type=int, default=1, help="run the serving leg (1/0)")
     p.add_argument("--serving-requests", type=int, default=120, help="requests at 200/s in the serving leg")
     p.add_argument("--radiography", type=int, default=1, help="run the radiography precision-ablation leg (1/0)")
@@ -193,12 +203,13 @@ def main():
         return
     import numpy as np
     import torch
-    if args.radiography_only:
+    if args.radiography_only or args.batched_only:
         from midsx_gb300 import build as B
         B.build()
         torch.cuda.set_device(local)
         if rank == 0:
-            print(json.dumps(radiography_leg(args, np, torch)), flush=True)
+            out = radiography_leg(args, np, torch) if args.radiography_only else batched_leg(args, torch)
+            print(json.dumps(out), flush=True)
         return
 
     import midsx_gb300 as M
@@ -220,7 +231,7 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     base = replica_first(rank, 0, 0)
 
-    def step(i, precision="mixed", n=N_hist, events=None):
+    def step(i, precision=args.precision, n=N_hist, events=None):
         flush.zero_()
         if events:
             events[0].record(stream)
@@ -253,9 +264,10 @@ def main():
     st = tl.stats()  # raises MidsxError(STEP_CAP) if any history reached the step cap
     result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
-              "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport / int64 fixed-point tallies",
+              "scaling": "weak", "vs_baseline": None,
+              "dtype": "f32 transport / int64 fixed-point tallies" if args.precision == "mixed" else "f64",
               "data": "synthetic (seeded ellipsoid phantom, Kramers spectrum)",
-              "config": {"workload": sc.name, "histories_per_step": N_hist, "precision": "mixed",
+              "config": {"workload": sc.name, "histories_per_step": N_hist, "precision": args.precision,
                          "voxels": ph.n_voxels, "dose_tally": "count/sum/sumsq per voxel (268 MB)",
                          "l2": "flushed between steps (256 MB write) and tally > L2",
                          "launch": "photon pool, 128-thread blocks, 2 Woodcock steps per pass (defaults)",
@@ -350,7 +362,17 @@ def main():
             "issue_active_pct": profile["issue_active_pct"],
             "warps_active_per_sm": profile.get("warps_active_per_sm"),
             "lanes_per_instruction": profile.get("lanes_per_instruction"),
-            "source": "ncu capture of 1e6 histories (profiles/transport_traffic.txt)"}
+            "l2_sectors_per_history": profile.get("l2_sectors_per_history"),
+            "l2_gbs_in_capture": profile.get("l2_gbs"),
+            "source": "ncu capture of 4e6 histories (profiles/transport_traffic.txt)"}
+    rs = random_sector_leg(torch)
+    result["roofline"]["random_sector"] = rs
+    # the same histories against the random-sector ceilings: voxel fetches from the L2 (the
+    # 8 MB phantom stays resident), tally records as atomics to HBM (the 268 MB tally does not)
+    bound = sector_bound_rate(F, W, rs["l2_load_gbs"], rs["hbm_red_gbs"])
+    result["roofline"]["random_sector_bound"] = {
+        "fetches_from": "L2", "tally_records_to": "HBM", "histories_per_s": bound,
+        "frac": value / world / bound}
     if "e2e" not in result:
         result["e2e"] = None
     if not args.quick:
@@ -361,6 +383,20 @@ def main():
         result["water_cube_plain"] = water_cube_leg(args, np, torch)
     if not args.quick and args.radiography:
         result["radiography_precision_ablation"] = radiography_leg(args, np, torch)
+    # configurations whose phantom and tallies fit the L2: frac of the L2 random-sector bound,
+    # with F and W frozen from the oracle's counters on their seeded inputs
+    wc = result.get("water_cube_plain")
+    if wc:
+        F1, W1 = FROZEN_FW["water_cube"]
+        b1 = sector_bound_rate(F1, W1, rs["l2_load_gbs"], rs["l2_red_gbs"])
+        wc["l2_random_sector_bound"] = {"F": F1, "W": W1, "histories_per_s": b1, "frac": wc["mixed"]["value"] / b1}
+    ra = result.get("radiography_precision_ablation")
+    if ra:
+        F3, W3 = FROZEN_FW["radiography"]
+        b3 = sector_bound_rate(F3, W3, rs["l2_load_gbs"], rs["l2_red_gbs"])
+        ra["l2_random_sector_bound"] = {"F": F3, "W": W3, "histories_per_s": b3,
+                                        "frac": ra["reference_tracking"]["mixed"]["value"] / b3,
+                                        "tracking": "reference (F counts its Woodcock steps in the grid)"}
     if not args.quick and args.batched:
         result["batched"] = batched_leg(args, torch)
     if not args.quick and args.serving:
@@ -545,15 +581,69 @@ def batch_variance_leg(M, np, torch, sc, tables, ph, src, sptr, flush, n_hist):
     return out
 
 
+# Voxel fetches (F) and tally records (W) per history counted by the oracle on the seeded
+# inputs of the water-cube (100^3, 60 keV pencil) and radiography (512x512x256, 16 Pb spheres,
+# reference tracking) workloads, frozen with the CPU baseline.
+FROZEN_FW = {"water_cube": (2.06, 2.15), "radiography": (2369.0, 1.23)}
+
+
+def sector_bound_rate(F, W, load_gbs, red_gbs):
+    """Histories/s if every voxel fetch and tally record ran at its random-32 B-sector ceiling."""
+    return 1.0 / (32.0 * F / (load_gbs * 1e9) + 32.0 * W / (red_gbs * 1e9))
+
+
+def random_sector_leg(torch, requests=1 << 27):
+    """Ceilings of random 32 B sector traffic (midsx_gpu_probe_sectors): loads cached in L2 only
+    and 64-bit atomic adds, over footprints from 16 MiB to 4 GiB; CUDA events around 5 launches
+    after 2 warm-up launches, `requests` sectors per launch.  The L2 ceiling is the best of the
+    footprints up to a quarter of the L2, the HBM ceiling the 4 GiB footprint."""
+    import ctypes as C
+    from midsx_gb300 import native as N
+    lib = N.load()
+    l2 = torch.cuda.get_device_properties(torch.cuda.current_device()).L2_cache_size
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    out = {"l2_bytes": l2, "requests_per_launch": requests, "load_gbs_by_footprint": {}, "red_gbs_by_footprint": {}}
+    for mib in (16, 32, 64, 256, 1024, 4096):
+        buf = torch.zeros(mib << 20, dtype=torch.uint8, device="cuda")
+        for mode, key in ((0, "load_gbs_by_footprint"), (1, "red_gbs_by_footprint")):
+            issued = C.c_uint64()
+
+            def launch(seed):
+                N.check(lib.midsx_gpu_probe_sectors(C.c_void_p(buf.data_ptr()), buf.numel(), mode, requests, seed,
+                                                    C.byref(issued), C.c_void_p(stream.cuda_stream)),
+                        "midsx_gpu_probe_sectors")
+            launch(1)
+            launch(2)
+            ev[0].record(stream)
+            for r in range(5):
+                launch(100 + r)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            t = ev[0].elapsed_time(ev[1]) / 1e3 / 5
+            out[key]["%d_MiB" % mib] = issued.value * 32 / t / 1e9
+            buf.zero_()
+        del buf
+    torch.cuda.empty_cache()
+    fits = [k for k in out["load_gbs_by_footprint"] if (int(k.split("_")[0]) << 20) <= l2 // 4]
+    out["l2_load_gbs"] = max(out["load_gbs_by_footprint"][k] for k in fits)
+    out["l2_red_gbs"] = max(out["red_gbs_by_footprint"][k] for k in fits)
+    out["hbm_load_gbs"] = out["load_gbs_by_footprint"]["4096_MiB"]
+    out["hbm_red_gbs"] = out["red_gbs_by_footprint"]["4096_MiB"]
+    return out
+
+
 def batched_leg(args, torch):
     """64 independent simulations (phantom edge log-uniform 32-256 voxels at 1 mm, 20-120 kVp,
-    1e5-1e8 histories each, own dose tallies) in one persistent launch: launch shape from the
-    autotuner, the launch captured in a CUDA graph and replayed; beside it the same jobs run
-    one midsx_gpu_run each, back to back on one stream."""
+    1e5-1e8 histories each, own dose tallies) in one CUDA-graph replay: the jobs of at least
+    the own-launch threshold in single-job launches of their own, the others in one persistent
+    launch (shape from the autotuner); beside it the same graph with every job in the
+    persistent launch, and the same jobs run one midsx_gpu_run each, back to back on one
+    stream."""
     import midsx_gb300 as M
     from midsx_gb300 import scenes
     t0 = time.time()
-    jobs = scenes.batch_jobs(n_jobs=64, seed=1, hist_scale=args.batch_scale)
+    jobs = scenes.batch_jobs(n_jobs=args.batch_jobs, seed=1, hist_scale=args.batch_scale)
     tables = M.Tables(jobs[0].materials, e_max=150e3)
     objs = []
     for sc in jobs:
@@ -563,7 +653,9 @@ def batched_leg(args, torch):
     batch = M.Batch(tables, [(ph, src, tl, 1 + j, 0, sc.n_histories)
                              for j, (sc, (ph, src, tl)) in enumerate(zip(jobs, objs))])
     stream = M.Stream()
-    launch, tuned_rate = batch.autotune("mixed", trial=4_000_000, stream=stream.handle)
+    launch, tuned_rate = {}, None
+    if args.batch_autotune:
+        launch, tuned_rate = batch.autotune("mixed", trial=4_000_000, stream=stream.handle)
     batch.capture(stream.handle, "mixed", **launch)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     ts = torch.cuda.ExternalStream(stream.handle.value)
@@ -576,6 +668,19 @@ def batched_leg(args, torch):
     ev[1].record(ts)
     stream.synchronize()
     graph_s = ev[0].elapsed_time(ev[1]) / 1e3 / reps
+    # the same graph with every job in the persistent launch (no launches of their own)
+    batch.set_own_launch(2**64 - 1)
+    batch.capture(stream.handle, "mixed", **launch)
+    batch.replay(stream.handle)
+    stream.synchronize()
+    ev[0].record(ts)
+    for _ in range(reps):
+        batch.replay(stream.handle)
+    ev[1].record(ts)
+    stream.synchronize()
+    persistent_s = ev[0].elapsed_time(ev[1]) / 1e3 / reps
+    batch.set_own_launch(0)
+    own_min = 57344 * torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     # the same jobs as separate single-simulation launches
     ev2 = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     ev2[0].record(ts)
@@ -587,12 +692,54 @@ def batched_leg(args, torch):
     stream.synchronize()
     seq_s = ev2[0].elapsed_time(ev2[1]) / 1e3
     h = batch.histories
-    out = {"workload": "64 jobs, edge 32-256 voxels at 1 mm, 20-120 kVp, histories log-uniform 1e5-1e8 x %g"
-                       % args.batch_scale,
+    out = {"workload": "%d jobs, edge 32-256 voxels at 1 mm, 20-120 kVp, histories log-uniform 1e5-1e8 x %g"
+                       % (args.batch_jobs, args.batch_scale),
            "histories_per_replay": h, "value": h / graph_s, "unit": UNIT, "ms_per_replay": 1e3 * graph_s,
            "separate_launches_value": h / seq_s, "autotuned_launch": launch, "autotune_trial_rate": tuned_rate,
+           "own_launch_jobs": sum(1 for sc in jobs if sc.n_histories >= own_min),
+           "own_launch_min_histories": own_min,
+           "own_launch_histories": sum(sc.n_histories for sc in jobs if sc.n_histories >= own_min),
+           "all_jobs_in_the_persistent_launch_value": h / persistent_s,
            "replays_timed": reps}
     batch.close()
+    if not args.batch_pair:
+        stream.close()
+        return out
+    # plain FP64 and mixed on the same jobs (histories x fp64_scale, so that the FP64 runs stay
+    # short): batched under a graph and as separate launches, each precision with its own tallies
+    scale64 = args.batch_fp64_scale
+    small = scenes.batch_jobs(n_jobs=args.batch_jobs, seed=1, hist_scale=args.batch_scale * scale64)
+    pair = {"histories_scale": args.batch_scale * scale64}
+    for prec in ("fp64", "mixed"):
+        tls = [M.Tallies(ph, sc.specs, sc.dose_mode) for sc, (ph, _, _) in zip(small, objs)]
+        b = M.Batch(tables, [(ph, src, tl, 1 + j, 0, sc.n_histories)
+                             for j, (sc, (ph, src, _), tl) in enumerate(zip(small, objs, tls))])
+        lp = {}
+        if args.batch_autotune:
+            lp, _ = b.autotune(prec, trial=1_000_000 if prec == "fp64" else 4_000_000, stream=stream.handle)
+        b.capture(stream.handle, prec, **lp)
+        b.replay(stream.handle)
+        stream.synchronize()
+        ev[0].record(ts)
+        b.replay(stream.handle)
+        ev[1].record(ts)
+        stream.synchronize()
+        g_s = ev[0].elapsed_time(ev[1]) / 1e3
+        ev2[0].record(ts)
+        for j, (sc, (ph, src, _), tl) in enumerate(zip(small, objs, tls)):
+            tl.reset(stream.handle)
+            M.run(tables, ph, src, tl, sc.n_histories, seed=1 + j, first=0, precision=prec, stream=stream.handle)
+        ev2[1].record(ts)
+        stream.synchronize()
+        s_s = ev2[0].elapsed_time(ev2[1]) / 1e3
+        pair[prec] = {"histories": b.histories, "batched_value": b.histories / g_s,
+                      "separate_launches_value": b.histories / s_s, "autotuned_launch": lp}
+        b.close()
+        for tl in tls:
+            tl.close()
+    pair["mixed_batched_over_fp64_separate"] = pair["mixed"]["batched_value"] / pair["fp64"]["separate_launches_value"]
+    pair["mixed_batched_over_fp64_batched"] = pair["mixed"]["batched_value"] / pair["fp64"]["batched_value"]
+    out["fp64_pair_same_jobs"] = pair
     stream.close()
     return out
 

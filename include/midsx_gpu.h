@@ -450,8 +450,19 @@ typedef struct midsx_batch_job {
 midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const midsx_batch_job* jobs, int32_t n_jobs,
                                     midsx_batch_h* out);
 midsx_status midsx_gpu_batch_destroy(midsx_batch_h b);
-/* One launch over every job (cfg: precision and launch shape; its seed/first/n are unused),
- * then the batch's epoch advances so that the next run transports the next histories. */
+/* Large jobs: a job of at least `min_histories` histories runs as a single-job launch of its
+ * own, ahead of the persistent launch of the others, on the same stream (and in the same
+ * captured graph); results are unchanged (same history ids and streams).  A long job gains
+ * nothing from sharing a launch - its own launch's tail is a small share of its time - and
+ * runs faster in the single-job kernel, whose job lives in the constant bank instead of
+ * shared memory.  0 restores the default, 32 loads of the GPU's resident photon slots
+ * (57,344 histories per SM: 8.7e6 on 152 SMs); UINT64_MAX keeps every job in the persistent
+ * launch.  Synchronous; call it outside a stream capture. */
+midsx_status midsx_gpu_batch_set_own_launch(midsx_batch_h b, uint64_t min_histories);
+/* One persistent launch over every job (cfg: precision and launch shape; its seed/first/n are
+ * unused) - the large jobs first in launches of their own (midsx_gpu_batch_set_own_launch),
+ * with the default single-job launch shape - then the batch's epoch advances so that the
+ * next run transports the next histories. */
 midsx_status midsx_gpu_batch_run(midsx_batch_h b, const midsx_run_config* cfg, void* stream);
 /* Captures one run (counter reset, persistent launch, epoch advance) into a CUDA graph on
  * `stream`; midsx_gpu_batch_replay launches it.  Replays advance the epoch like runs. */
@@ -600,6 +611,18 @@ midsx_status midsx_gpu_trace_deposits_noalloc(midsx_tables_h tables, midsx_phant
  * FP32 node array (a self-check of the FP32 bucket tables). */
 midsx_status midsx_gpu_table_index(midsx_tables_h tables, int32_t material, const double* e,
                                    int64_t n, int64_t* idx);
+
+/* ------------------------------------------------------------ measurement probe --- */
+/* Random 32 B sector probe (measurement only; no reference counterpart).  Enqueues on
+ * `stream` about `requests` accesses to pseudo-random 32 B sectors of the device buffer
+ * `buf`: mode 0 loads 4 bytes cached in L2 only, mode 1 adds 1 to a 64-bit word (a device
+ * atomic whose result is unused).  These are the transport kernel's access forms (voxel-ID
+ * fetches, tally read-modify-writes); timed over a footprint that fits the L2 and one that
+ * does not, they give the L2 and HBM ceilings for that traffic.  `bytes`: a power of two from
+ * 32 to 2^37; `buf` 32-byte aligned.  *issued receives the request count actually enqueued
+ * (rounded up to fill the launch). */
+midsx_status midsx_gpu_probe_sectors(void* buf, uint64_t bytes, int32_t mode, uint64_t requests,
+                                     uint32_t seed, uint64_t* issued, void* stream);
 
 #ifdef __cplusplus
 }

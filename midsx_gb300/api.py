@@ -457,6 +457,13 @@ class Batch:
     def histories(self):
         return sum(int(j[5]) for j in self.jobs)
 
+    def set_own_launch(self, min_histories=0):
+        """Jobs of at least min_histories run as single-job launches of their own ahead of the
+        persistent launch (0: the default threshold; 2**64 - 1: every job in the persistent
+        launch).  Results are unchanged."""
+        N.check(N.load().midsx_gpu_batch_set_own_launch(self.handle, int(min_histories)),
+                "midsx_gpu_batch_set_own_launch")
+
     def run(self, precision="mixed", stream=None, **launch):
         cfg = run_config(0, 0, 0, precision, **launch)
         N.check(N.load().midsx_gpu_batch_run(self.handle, C.byref(cfg), stream), "midsx_gpu_batch_run")

@@ -99,6 +99,7 @@ def build(verbose=False, with_oracle=True):
     units = [
         ("transport.cu", [nvcc] + NVCC_FLAGS),
         ("server.cu", [nvcc] + NVCC_FLAGS),
+        ("probe.cu", [nvcc] + NVCC_FLAGS),
         ("tables.cpp", ["g++"] + CXX_FLAGS),
     ]
     core_units = [f for f in sorted(os.listdir(CSRC)) if f.startswith("core_") and f.endswith(".cpp")]

@@ -32,6 +32,14 @@ __device__ __forceinline__ R refresh_energy(const RunParams& P, R E, R* thr, R* 
     return mu_max;
 }
 
+// The same, out of line: the single-job FP32 photon-pool kernel calls this copy (+0.8 % on
+// the cone-beam dose workload: one copy of the M + 1 table lookups in the kernel's code); the
+// batched kernel keeps the inlined one (out of line there: -2.7 %).
+template <typename R>
+__device__ __noinline__ R refresh_energy_call(const RunParams& P, R E, R* thr, R* mu, int stride) {
+    return refresh_energy<R>(P, E, thr, mu, stride);
+}
+
 // setInteractionType's probabilities (physics_engine.cpp:82-109): coherent and incoherent
 // cross sections (LogLogSpline) over the material's total, at one energy key.  (Inlined: an
 // out-of-line copy measured 4-5 % slower, the call saving registers around it.)

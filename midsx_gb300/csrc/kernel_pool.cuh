@@ -642,7 +642,10 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
         }
         // per-energy cache of Compton survivors and new histories, in one call
         if (need_refresh) {
-            mu_max = refresh_energy<R>(P, E, S.thr + sl, S.mu + sl, ns);
+            if constexpr (MULTI || !MX)
+                mu_max = refresh_energy<R>(P, E, S.thr + sl, S.mu + sl, ns);
+            else
+                mu_max = refresh_energy_call<R>(P, E, S.thr + sl, S.mu + sl, ns);
             inv_mu_max = R(1) / mu_max;
         }
         // survivors and new histories go to the ready list

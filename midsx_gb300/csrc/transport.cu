@@ -2120,6 +2120,14 @@ struct midsx_gpu_batch {
     cudaGraphExec_t graph = nullptr;
     int graph_precision = -1;
     double max_energy = 0;
+    // large jobs in launches of their own (midsx_gpu_batch_set_own_launch); the persistent
+    // launch takes the others, through their own record and prefix arrays
+    uint64_t own_min = 0;
+    std::vector<int> own;
+    std::vector<unsigned long long> host_rest_prefix;
+    int n_rest = 0;
+    DevJob* rest_jobs = nullptr;
+    unsigned long long* rest_prefix = nullptr;
 };
 
 namespace {
@@ -2135,6 +2143,34 @@ void batch_params(const midsx_gpu_batch* b, RunParams& P, const unsigned long lo
     P.epoch = b->words;
     for (auto* t : b->tallies) P.spectra |= t->spectra;
     for (const DevJob& j : b->host_jobs) P.max_steps = std::max(P.max_steps, int(j.step_cap));
+}
+
+// Splits the jobs into those with a launch of their own (n >= min) and the rest, whose
+// records and history prefix go to device arrays of their own.  Synchronous.
+midsx_status batch_split(midsx_gpu_batch* b, uint64_t min_histories) {
+    if (min_histories == 0) min_histories = uint64_t(57344) * uint64_t(std::max(1, b->tables->sm_count));
+    std::vector<int> own;
+    std::vector<DevJob> rest;
+    std::vector<unsigned long long> rest_prefix(1, 0);
+    for (int i = 0; i < b->n_jobs; ++i) {
+        const DevJob& d = b->host_jobs[size_t(i)];
+        if (d.n >= min_histories) {
+            own.push_back(i);
+        } else {
+            rest.push_back(d);
+            rest_prefix.push_back(rest_prefix.back() + d.n);
+        }
+    }
+    if (!rest.empty()) {
+        CUDA_TRY(cudaMemcpy(b->rest_jobs, rest.data(), rest.size() * sizeof(DevJob), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(b->rest_prefix, rest_prefix.data(), rest_prefix.size() * sizeof(unsigned long long),
+                            cudaMemcpyHostToDevice));
+    }
+    b->own_min = min_histories;
+    b->own = own;
+    b->n_rest = int(rest.size());
+    b->host_rest_prefix = rest_prefix;
+    return MIDSX_OK;
 }
 
 midsx_status batch_check_precision(midsx_gpu_batch* b, int precision) {
@@ -2155,13 +2191,40 @@ midsx_status batch_check_precision(midsx_gpu_batch* b, int precision) {
     return MIDSX_OK;
 }
 
-// One batched launch followed by the epoch advance (both on `s`).
+// One run of the batch on `s`: the large jobs' own launches (single-job kernel, default
+// launch shape, the batch's epoch and history counter words), the persistent launch over the
+// rest, then the epoch advance.
 midsx_status batch_enqueue(midsx_gpu_batch* b, const midsx_run_config& cfg, cudaStream_t s) {
-    RunParams P;
-    batch_params(b, P, b->prefix, b->host_prefix.back());
-    if (P.total == 0) return MIDSX_OK;
-    midsx_status st = launch_kernel(b->tables, P, cfg, true, s);
-    if (st != MIDSX_OK) return st;
+    if (b->host_prefix.back() == 0) return MIDSX_OK;
+    midsx_run_config single = cfg;
+    single.block_size = single.blocks_per_sm = single.regroup = single.chunk = 0;
+    single.scheduler = MIDSX_SCHED_DEFAULT;
+    single.steps_per_pass = single.pass_repeats = 0;
+    for (int j : b->own) {
+        RunParams Q;
+        std::memset(&Q, 0, sizeof(Q));
+        Q.T = b->tables->T;
+        Q.job0 = b->host_jobs[size_t(j)];
+        philox_round_keys(Q.job0.seed, Q.round_keys);
+        Q.geo_f = make_geo<float>(Q.job0.G);
+        Q.geo_d = make_geo<double>(Q.job0.G);
+        Q.n_jobs = 1;
+        Q.max_steps = int(Q.job0.step_cap);
+        Q.counter = b->words + 1;
+        Q.total = Q.job0.n;
+        Q.epoch = b->words;  // history ids first + epoch * n + i, as in the persistent launch
+        Q.spectra = b->tallies[size_t(j)]->spectra;
+        midsx_status st = launch_kernel(b->tables, Q, single, false, s);
+        if (st != MIDSX_OK) return st;
+    }
+    if (b->host_rest_prefix.back() > 0) {
+        RunParams P;
+        batch_params(b, P, b->rest_prefix, b->host_rest_prefix.back());
+        P.jobs = b->rest_jobs;
+        P.n_jobs = b->n_rest;
+        midsx_status st = launch_kernel(b->tables, P, cfg, true, s);
+        if (st != MIDSX_OK) return st;
+    }
     advance_epoch_kernel<<<1, 1, 0, s>>>(b->words);
     CUDA_TRY(cudaGetLastError());
     return MIDSX_OK;
@@ -2197,15 +2260,24 @@ extern "C" midsx_status midsx_gpu_batch_create(midsx_tables_h tables, const mids
     }
     if (!cuda_ok(cudaMalloc(&b->jobs, n_jobs * sizeof(DevJob)), "cudaMalloc") ||
         !cuda_ok(cudaMalloc(&b->prefix, (n_jobs + 1) * sizeof(unsigned long long)), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&b->words, (2 + kMaxBatchJobs) * sizeof(unsigned long long)), "cudaMalloc"))
+        !cuda_ok(cudaMalloc(&b->words, (2 + kMaxBatchJobs) * sizeof(unsigned long long)), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&b->rest_jobs, n_jobs * sizeof(DevJob)), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&b->rest_prefix, (n_jobs + 1) * sizeof(unsigned long long)), "cudaMalloc"))
         return MIDSX_OOM;
     CUDA_TRY(cudaMemcpy(b->jobs, b->host_jobs.data(), n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(b->prefix, b->host_prefix.data(), (n_jobs + 1) * sizeof(unsigned long long),
                         cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemset(b->words, 0, (2 + kMaxBatchJobs) * sizeof(unsigned long long)));
+    midsx_status sst = batch_split(b, 0);
+    if (sst != MIDSX_OK) return sst;
     guard.release();
     *out = b;
     return MIDSX_OK;
+}
+
+extern "C" midsx_status midsx_gpu_batch_set_own_launch(midsx_batch_h b, uint64_t min_histories) {
+    if (!b) return MIDSX_INVALID_ARG;
+    return batch_split(b, min_histories);
 }
 
 extern "C" midsx_status midsx_gpu_batch_destroy(midsx_batch_h b) {
@@ -2214,6 +2286,8 @@ extern "C" midsx_status midsx_gpu_batch_destroy(midsx_batch_h b) {
     cudaFree(b->jobs);
     cudaFree(b->prefix);
     cudaFree(b->words);
+    cudaFree(b->rest_jobs);
+    cudaFree(b->rest_prefix);
     delete b;
     return MIDSX_OK;
 }

@@ -180,11 +180,14 @@ _SIGNATURES = {
     "midsx_gpu_sample": (C.c_int, [VP, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64,
                                    C.c_uint64, C.c_int64, PD, PD]),
     "midsx_gpu_table_index": (C.c_int, [VP, C.c_int32, PD, C.c_int64, PI64]),
+    "midsx_gpu_probe_sectors": (C.c_int, [VP, C.c_uint64, C.c_int32, C.c_uint64, C.c_uint32,
+                                         C.POINTER(C.c_uint64), VP]),
     "midsx_gpu_stream_create": (C.c_int, [C.POINTER(VP)]),
     "midsx_gpu_stream_destroy": (C.c_int, [VP]),
     "midsx_gpu_stream_synchronize": (C.c_int, [VP]),
     "midsx_gpu_batch_create": (C.c_int, [VP, C.POINTER(BatchJob), C.c_int32, C.POINTER(VP)]),
     "midsx_gpu_batch_destroy": (C.c_int, [VP]),
+    "midsx_gpu_batch_set_own_launch": (C.c_int, [VP, C.c_uint64]),
     "midsx_gpu_batch_run": (C.c_int, [VP, C.POINTER(RunConfig), VP]),
     "midsx_gpu_batch_capture": (C.c_int, [VP, C.POINTER(RunConfig), VP]),
     "midsx_gpu_batch_replay": (C.c_int, [VP, VP]),

@@ -124,6 +124,52 @@ def test_graph_replays_advance_epochs(setup):
         assert a[3]["histories"] == 2 * sc.n_histories
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_large_jobs_in_launches_of_their_own_equal_single_runs(setup, precision):
+    """With the own-launch threshold between the jobs' sizes, the large jobs run single-job
+    launches inside the batch run and its captured graph: two replays still equal single
+    runs over [first, first + 2n) (history ids from the batch's epoch), job by job."""
+    tables, jobs = setup
+    sizes = sorted(sc.n_histories for sc in jobs)
+    threshold = sizes[len(sizes) // 2]
+    assert sizes[0] < threshold <= sizes[-1]
+    stream = M.Stream()
+    objs = [make(tables, sc) for sc in jobs]
+    batch = M.Batch(tables, [(ph, src, tl, 60 + j, 500 * j, sc.n_histories)
+                             for j, (sc, (ph, src, tl)) in enumerate(zip(jobs, objs))])
+    batch.set_own_launch(threshold)
+    batch.capture(stream.handle, precision)
+    batch.replay(stream.handle)
+    batch.replay(stream.handle)
+    stream.synchronize()
+    for j, sc in enumerate(jobs):
+        ph, src, tl = make(tables, sc)
+        M.run(tables, ph, src, tl, 2 * sc.n_histories, seed=60 + j, first=500 * j, precision=precision)
+        a, b = results(objs[j][2]), results(tl)
+        if precision == "mixed":
+            for x, y in zip(a[:3], b[:3]):
+                np.testing.assert_array_equal(x, y)
+        else:
+            np.testing.assert_allclose(a[0], b[0], rtol=1e-9, atol=1e-6)
+            np.testing.assert_array_equal(a[2], b[2])
+        assert a[3]["histories"] == b[3]["histories"] == 2 * sc.n_histories
+        assert a[3]["steps"] == b[3]["steps"]
+    # every job in launches of its own, then none
+    for t in (1, 2**64 - 1):
+        objs2 = [make(tables, sc) for sc in jobs[:2]]
+        b2 = M.Batch(tables, [(ph, src, tl, 60 + j, 500 * j, sc.n_histories)
+                              for j, (sc, (ph, src, tl)) in enumerate(zip(jobs[:2], objs2))])
+        b2.set_own_launch(t)
+        b2.run(precision)
+        for j, sc in enumerate(jobs[:2]):
+            ph, src, tl = make(tables, sc)
+            M.run(tables, ph, src, tl, sc.n_histories, seed=60 + j, first=500 * j, precision=precision)
+            assert results(objs2[j][2])[3]["steps"] == results(tl)[3]["steps"]
+        b2.close()
+    batch.close()
+    stream.close()
+
+
 def test_autotune_picks_a_shape_and_resets_tallies(setup):
     tables, jobs = setup
     objs = [make(tables, sc) for sc in jobs]
