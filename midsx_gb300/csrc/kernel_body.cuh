@@ -78,6 +78,36 @@ __device__ __forceinline__ bool sample_compton(const RunParams& P, const DevMate
     const R k = E / R(kMec2);
     const R r1p = (R(1) + R(2) * k) / (R(9) + R(2) * k);
     const R s_max = lin_lookup<R>(P.T, Mt.sfunc, alpha * k * sqrt_(R(2)));
+    if constexpr (sizeof(R) == 4) {
+        // The same trial with one division instead of six to eight: with b = 1 + 2k r2 and
+        // a = 1 + 2k, chi = b (first branch) or a / b (second), 1/chi = b / a there, and
+        // 1/k - 1/kp = (1 - chi)/k; 1/k, 1/a and 1/s_max are taken once per event.  Equal to
+        // the form below up to rounding (+2.5 % on the cone-beam dose workload); the FP64
+        // form keeps the reference's expressions, operation for operation.
+        const R ik = R(1) / k, k2 = R(2) * k, a = R(1) + k2, ia = R(1) / a, is_max = R(1) / s_max;
+        for (int trial = 0; trial < P.max_trials; ++trial) {
+            ++trials;
+            R r1 = uniform<R>(rng), r2 = uniform<R>(rng), r3 = uniform<R>(rng);
+            R chi, ichi;
+            const R b = R(1) + k2 * r2;
+            if (r1 <= r1p) {
+                chi = b;
+                ichi = R(1) / chi;
+                if (!(r3 <= R(4) * ichi * (R(1) - ichi))) continue;
+            } else {
+                ichi = b * ia;
+                chi = a / b;
+                R tt = (R(1) - chi) * ik + R(1);
+                if (!(R(2) * r3 <= tt * tt + ichi)) continue;
+            }
+            kp = k * ichi;
+            mu = R(1) + (R(1) - chi) * ik;
+            R x = alpha * k * sqrt_(R(1) - mu);
+            R accept = lin_lookup<R>(P.T, Mt.sfunc, x) * is_max;
+            if (uniform<R>(rng) <= accept) return true;
+        }
+        return false;
+    }
     for (int trial = 0; trial < P.max_trials; ++trial) {
         ++trials;
         R r1 = uniform<R>(rng), r2 = uniform<R>(rng), r3 = uniform<R>(rng);

@@ -105,7 +105,8 @@ struct midsx_gpu_server {
 
     cudaMemPool_t pool = nullptr;
     cudaStream_t setup = nullptr;
-    cudaEvent_t setup_done = nullptr;
+    cudaEvent_t setup_done = nullptr;  // recorded after each batch of setup work
+    bool setup_recorded = false;
     Slot slots[kMaxSlots];
 
     std::mutex mu;
@@ -130,7 +131,7 @@ struct midsx_gpu_server {
     void run();
     bool retire_locked();
     bool admit_locked(bool& enqueued_setup);
-    bool launch_locked(bool setup_pending);
+    bool launch_locked();
     void fail_locked(Request* r, midsx_status s, const std::string& why);
     void unpin_locked(Request* r);
     void free_request_memory_locked(Request* r);
@@ -305,7 +306,7 @@ bool midsx_gpu_server::admit_locked(bool& enqueued_setup) {
 }
 
 // Fills free slots with launches over the admitted requests that have histories left.
-bool midsx_gpu_server::launch_locked(bool setup_pending) {
+bool midsx_gpu_server::launch_locked() {
     bool changed = false;
     const size_t rec = midsx::rt::job_record_bytes();
     for (int i = 0; i < n_slots && !broken; ++i) {
@@ -391,7 +392,10 @@ bool midsx_gpu_server::launch_locked(bool setup_pending) {
                     ok(cudaMemcpyAsync(s.dev_prefix, s.host_prefix, size_t(nj + 1) * 8, cudaMemcpyHostToDevice,
                                        s.stream),
                        "cudaMemcpyAsync");
-        if (good && setup_pending) good = ok(cudaStreamWaitEvent(s.stream, setup_done, 0), "cudaStreamWaitEvent");
+        // every launch waits for the setup work recorded so far (uploads, zeroed tallies): a
+        // request admitted in an earlier pass of the scheduler may take its first launch now,
+        // while the setup stream is still working through a large upload or memset
+        if (good && setup_recorded) good = ok(cudaStreamWaitEvent(s.stream, setup_done, 0), "cudaStreamWaitEvent");
         if (good) good = ok(cudaEventRecord(s.start, s.stream), "cudaEventRecord");
         bool spectra = false;
         for (auto& p : s.parts) spectra |= midsx::rt::tallies_spectra(p.req->tallies);
@@ -449,9 +453,12 @@ void midsx_gpu_server::run() {
         } else {
             changed |= admit_locked(setup_enqueued);
             if (setup_enqueued) {
-                if (!ok(cudaEventRecord(setup_done, setup), "cudaEventRecord")) broken = true;
+                if (!ok(cudaEventRecord(setup_done, setup), "cudaEventRecord"))
+                    broken = true;
+                else
+                    setup_recorded = true;
             }
-            changed |= launch_locked(setup_enqueued);
+            changed |= launch_locked();
         }
         st.queued = int32_t(queue.size());
         st.active = int32_t(active.size());

@@ -1,12 +1,13 @@
 """Load driver for the request server: registers the serving mix's phantoms, submits a
-seeded Poisson stream of requests at their arrival times from one thread, and retires them
-from another (reads each result to host memory, then releases it).  Reports throughput and
-request latencies.
+seeded Poisson stream of requests at their arrival times from one thread, polls them from
+another and retires them from a few reader threads (each reads results to host memory on a
+stream of its own, then releases the request).  Reports throughput and request latencies.
 
 Latency of a request = time from its arrival (submission) to the moment its results are in
 host memory; the server-side part (submission to the end of its last launch) is reported
 beside it.
 """
+import queue
 import threading
 import time
 
@@ -48,26 +49,30 @@ class Mix:
         return self.server.submit(self.pid[key], self.source[key], req["n"], req["seed"], req.get("first", 0),
                                   precision, sc.specs, sc.dose_mode)
 
-    def read(self, rid, req):
-        """Results of a done request in host memory (dose arrays or detector images)."""
+    def read(self, rid, req, stream=None):
+        """Results of a done request in host memory (dose arrays or detector images), copied on
+        `stream` (None: the legacy default stream)."""
         sc = self.templates[req["cls"]][req["template"]]
         tl = self.server.tallies(rid)
         # a history that reached a cap is counted and reported by drive(), not raised here
-        out = {"stats": tl.stats(allow_cap=True)}
+        out = {"stats": tl.stats(stream, allow_cap=True)}
         if sc.dose_mode:
-            out["dose"] = tl.dose()
+            out["dose"] = tl.dose(stream)
         for i, spec in enumerate(sc.specs):
             if spec["kind"] == "binned":
-                out["binned%d" % i] = tl.binned(i)
+                out["binned%d" % i] = tl.binned(i, stream)
         return out
 
     def close(self):
         self.server.close()
 
 
-def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3600.0):
+def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3600.0, readers=4):
     """Plays `requests` (scenes.serving_requests) against mix.server in real time.  Returns a
-    dict of per-request records and summary figures; keep=True also returns the results."""
+    dict of per-request records and summary figures; keep=True also returns the results.
+    One thread polls the submitted requests; `readers` threads read finished ones to host
+    memory, each on a non-blocking stream of its own, so that a burst of requests finishing
+    at the end of one launch is not read one after another (ctypes calls release the GIL)."""
     n = len(requests)
     rids = [None] * n
     t_arr = [None] * n
@@ -77,13 +82,15 @@ def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3
     caps = [None] * n
     errors = []
     submitted = threading.Semaphore(0)
+    finished = queue.Queue()
+    readers = max(1, int(readers))
 
-    def retire():
-        pending = []  # indices of submitted, not yet retired requests
+    def poll():
+        pending = []  # indices of submitted requests not finished yet
         next_idx = 0
-        got = 0
+        seen = 0
         deadline = time.perf_counter() + timeout
-        while got < n and time.perf_counter() < deadline:
+        while seen < n and time.perf_counter() < deadline:
             while submitted.acquire(blocking=False):
                 pending.append(next_idx)
                 next_idx += 1
@@ -91,25 +98,43 @@ def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3
             for i in list(pending):
                 info = mix.server.poll(rids[i])
                 if info["state"] in (N.REQ_DONE, N.REQ_FAILED):
-                    if info["state"] == N.REQ_DONE:
-                        res = mix.read(rids[i], requests[i])
+                    infos[i] = info
+                    pending.remove(i)
+                    seen += 1
+                    finished.put(i)
+                    progressed = True
+            if not progressed:
+                time.sleep(poll_s)
+        for _ in range(readers):
+            finished.put(None)
+
+    def read():
+        stream = api.Stream()
+        try:
+            while True:
+                i = finished.get()
+                if i is None:
+                    break
+                if infos[i]["state"] == N.REQ_DONE:
+                    try:
+                        res = mix.read(rids[i], requests[i], stream.handle)
+                    except N.MidsxError as e:  # e.g. an energy left the tables: the request failed
+                        errors.append((i, e.status))
+                    else:
                         st = res["stats"]
                         caps[i] = (st["step_cap_hits"], st["compton_cap_hits"])
                         if keep:
                             results[i] = res
-                    else:
-                        errors.append((i, info["status"]))
-                    t_host[i] = time.perf_counter()
-                    infos[i] = info
-                    mix.server.release(rids[i])
-                    pending.remove(i)
-                    got += 1
-                    progressed = True
-            if not progressed:
-                time.sleep(poll_s)
+                else:
+                    errors.append((i, infos[i]["status"]))
+                t_host[i] = time.perf_counter()
+                mix.server.release(rids[i])
+        finally:
+            stream.close()
 
-    th = threading.Thread(target=retire)
-    th.start()
+    threads = [threading.Thread(target=poll)] + [threading.Thread(target=read) for _ in range(readers)]
+    for th in threads:
+        th.start()
     t0 = time.perf_counter()
     for i, req in enumerate(requests):
         delay = t0 + req["t"] - time.perf_counter()
@@ -118,7 +143,8 @@ def drive(mix, requests, precision="mixed", keep=False, poll_s=0.0005, timeout=3
         t_arr[i] = time.perf_counter()
         rids[i] = mix.submit(req, precision)
         submitted.release()
-    th.join()
+    for th in threads:
+        th.join()
     t_end = max(t for t in t_host if t is not None)
     lat = np.array([t_host[i] - t_arr[i] for i in range(n) if t_host[i] is not None])
     srv = np.array([infos[i]["t_done"] - infos[i]["t_submit"] for i in range(n) if infos[i] is not None])
