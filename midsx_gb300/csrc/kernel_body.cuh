@@ -181,7 +181,7 @@ __device__ __forceinline__ R box_entry(const V3<R>& p, const V3<R>& d, const V3<
         }
         R t1, t2;
         if constexpr (sizeof(R) == 4) {
-            const R id = R(1) / dd[a];
+            const R id = adiv(R(1), dd[a]);
             t1 = (ll[a] - pp[a]) * id;
             t2 = (ll[a] + ee[a] - pp[a]) * id;
         } else {
@@ -248,7 +248,7 @@ __device__ __forceinline__ void box_span(const V3<R>& p, const V3<R>& d, const V
         }
         R u1, u2;
         if constexpr (sizeof(R) == 4) {
-            const R id = R(1) / dd[a];
+            const R id = adiv(R(1), dd[a]);
             u1 = (ll[a] - pp[a]) * id;
             u2 = (ll[a] + ee[a] - pp[a]) * id;
         } else {
@@ -339,7 +339,7 @@ __device__ __forceinline__ int cell_flight(const Geo<R>& g, const DevGeom& D, co
     for (int a = 0; a < 3; ++a) {
         R q;
         if constexpr (sizeof(R) == 4)
-            q = (pp[a] + tin * dd[a] - oo[a]) * (R(1) / csz[a]);
+            q = (pp[a] + tin * dd[a] - oo[a]) * adiv(R(1), csz[a]);
         else
             q = (pp[a] + tin * dd[a] - oo[a]) / csz[a];
         int ci = q >= R(0) ? int(q) : 0;
@@ -349,7 +349,7 @@ __device__ __forceinline__ int cell_flight(const Geo<R>& g, const DevGeom& D, co
             inc3[a] = stride3;
             left3[a] = cn[a] - 1 - ci;
             if constexpr (sizeof(R) == 4) {
-                const R id = R(1) / dd[a];
+                const R id = adiv(R(1), dd[a]);
                 tn3[a] = (oo[a] + R(ci + 1) * csz[a] - pp[a]) * id;
                 dt3[a] = csz[a] * id;
             } else {
@@ -360,7 +360,7 @@ __device__ __forceinline__ int cell_flight(const Geo<R>& g, const DevGeom& D, co
             inc3[a] = -stride3;
             left3[a] = ci;
             if constexpr (sizeof(R) == 4) {
-                const R id = R(1) / dd[a];
+                const R id = adiv(R(1), dd[a]);
                 tn3[a] = (oo[a] + R(ci) * csz[a] - pp[a]) * id;
                 dt3[a] = -csz[a] * id;
             } else {
@@ -401,7 +401,7 @@ __device__ __forceinline__ int cell_flight(const Geo<R>& g, const DevGeom& D, co
         tn = tn > t ? tn : t;
         const R depth = mc * (tn - t);
         if (tau < depth) {
-            s = t + tau / mc;
+            s = t + adiv(tau, mc);
             mu_c = mc;
             return 0;
         }
