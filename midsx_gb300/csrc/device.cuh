@@ -140,10 +140,20 @@ MIDSX_HD Philox4 philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_
     return o;
 }
 
-// One random stream per history: draw n uses 64 bits of Philox block (n >> 1) with
-// counter (n >> 1, history_lo, history_hi, 0) and key (seed_lo, seed_hi).  The FP64 path
-// uses the top 53 bits, the FP32 path the top 24 bits of the same 64-bit word, so both
-// precisions consume identical streams.
+// One random stream per history h, key (seed_lo, seed_hi), with two kinds of draws:
+//   * event draws (source, interaction type, samplers, azimuths): draw n is the 64-bit half
+//     (n & 1) of Philox block (n >> 1, h_lo, h_hi, 0); every interaction starts a new block
+//     (align_event: n rounded up to even);
+//   * Woodcock-step draws: the step's free-path and delta-test uniforms are the 32-bit word
+//     pair (2 (i & 1), 2 (i & 1) + 1) of block (i >> 1, h_lo, h_hi, 1 + n), n the event
+//     draws so far (constant along a flight segment - the steps between two interactions -
+//     and different for every segment), i = (the history's Woodcock steps so far) + p, p the
+//     parity of that count at the segment's start, so that a segment starts on a block
+//     boundary and two steps share one block.  The photon-pool kernel's passes of two steps
+//     compute one block per pass.
+// The FP64 path uses the top 53 bits of a 64-bit draw (of a step word: its 32 bits, so a free
+// path is cut at -ln 2^-32 = 22.2 mean free paths, which a step passes with probability
+// 2.3e-10), the FP32 path the top 24 bits, so both precisions consume identical streams.
 struct HistoryRng {
     uint32_t k0, k1, h0, h1;
     uint32_t n;
@@ -192,6 +202,14 @@ struct HistoryRng {
         b1 = w.v[3];
         n = 2u * blk + 2u;
     }
+    // The Philox block of Woodcock step index i (the step stream above), with the key
+    // schedule precomputed (philox_round_keys of the seed) or computed as it goes.
+    MIDSX_HD Philox4 step_block_rk(uint32_t i, const uint32_t (&rk)[20]) const {
+        return philox4x32_10_rk(i >> 1, h0, h1, 1u + n, rk);
+    }
+    MIDSX_HD Philox4 step_block(uint32_t i) const { return philox4x32_10(i >> 1, h0, h1, 1u + n, k0, k1); }
+    // An interaction's first event draw starts a new block.
+    MIDSX_HD void align_event() { n = (n + 1u) & ~1u; }
     // next_pair64 with the stream's key schedule precomputed (philox_round_keys of its seed)
     MIDSX_HD void next_pair64_rk(uint64_t& first, uint64_t& second, const uint32_t (&rk)[20]) {
         uint32_t blk = (n + 1u) >> 1;

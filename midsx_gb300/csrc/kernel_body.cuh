@@ -540,6 +540,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
     R E = R(0), mu_max = R(0), inv_mu_max = R(0), s = R(0);
     int n_coh = 0, n_incoh = 0, vox = -1, mat = 0;
     uint32_t steps = 0, fetches = 0, trials = 0, words = 0;
+    uint32_t spar = 0u;  // step parity at the start of the flight segment (HistoryRng)
     R hist_dep = R(0);
     unsigned mask = 0xffffffffu;
 
@@ -567,9 +568,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
                 stat_add(st, kStStepCap, 1);
                 finish = true;
             } else {
+                // the step's uniforms: word pair (0, 1) or (2, 3) of its block (HistoryRng)
+                const uint32_t si = steps + spar;
                 ++steps;
-                uint64_t w1, w2;
-                rng.next_pair64(w1, w2);
+                const Philox4 q = rng.step_block(si);
+                const uint64_t w1 = uint64_t((si & 1u) ? q.v[2] : q.v[0]) << 32;
+                const uint64_t w2 = uint64_t((si & 1u) ? q.v[3] : q.v[1]) << 32;
                 // getFreePath.  The FP32 form uses the hardware log2 (absolute error ~1e-7 near
                 // U = 1, clamped at zero so that a step never goes backwards).
                 if constexpr (MX)
@@ -653,6 +657,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
                     stat_add(sj, kStSourceE, fx_stat(E));
                     n_coh = n_incoh = 0;
                     steps = fetches = trials = words = 0;
+                    spar = 0u;
                     hist_dep = R(0);
                     mu_max = refresh_energy<R>(P, E, thr, mucache, stride);
                     inv_mu_max = R(1) / mu_max;
@@ -665,6 +670,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
                 const R mu_tot = mucache[mat * stride];
                 R p_coh, p_incoh;
                 interaction_probs<R>(P.T, Mt, E, mu_tot, p_coh, p_incoh);
+                rng.align_event();
                 const R u3 = uniform<R>(rng);
                 const int cls0 = scatter_class(n_coh, n_incoh);
                 const R E0 = E;
@@ -737,6 +743,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) transport_kernel(
                         }
                     }
                 }
+                spar = steps & 1u;  // a new flight segment (HistoryRng)
                 if (finish) end_history();
             }
         }

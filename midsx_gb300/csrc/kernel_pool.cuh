@@ -46,10 +46,12 @@ constexpr uint32_t kKindFlight = 0u;  // slot kinds (meta bits 30-31)
 constexpr uint32_t kKindCollide = 1u;
 constexpr uint32_t kKindStart = 2u;
 
-// meta word of a slot: job (bits 0-7), material (8-15), coherent (16-22) and incoherent
-// (23-29) scatter counts saturated at 127 (only 0, 1 and "more" matter: scatter_class), kind.
-__device__ __forceinline__ uint32_t pack_meta(int job, int mat, int n_coh, int n_incoh, uint32_t kind) {
-    return uint32_t(job) | (uint32_t(mat) << 8) | (uint32_t(min(n_coh, 127)) << 16) |
+// meta word of a slot: job (bits 0-7), material (8-15), coherent (16-21) and incoherent
+// (23-29) scatter counts saturated at 63 and 127 (only 0, 1 and "more" matter:
+// scatter_class), the flight segment's step parity (22: HistoryRng), kind (30-31).
+__device__ __forceinline__ uint32_t pack_meta(int job, int mat, int n_coh, int n_incoh, uint32_t kind,
+                                              uint32_t par = 0u) {
+    return uint32_t(job) | (uint32_t(mat) << 8) | (uint32_t(min(n_coh, 63)) << 16) | (par << 22) |
            (uint32_t(min(n_incoh, 127)) << 23) | (kind << 30);
 }
 
@@ -245,6 +247,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
     HistoryRng rng;
     int job = 0, mat = 0, vox = -1, n_coh = 0, n_incoh = 0, ntal = 0;
     uint32_t kind = kKindFlight, steps = 0, fetches = 0, trials = 0, words = 0;
+    uint32_t spar = 0u;  // step parity at the start of the flight segment (HistoryRng)
+    uint32_t sw2 = 0u, sw3 = 0u;  // the step block's second word pair, for the pass's next step
 
     // Slot traffic is kept to the fields each transition needs.  In flight a photon changes
     // only its position, Philox position and counters; the collision site (step start, length,
@@ -257,7 +261,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
         inv_mu_max = R(1) / mu_max;
         const uint32_t meta = S.meta[sl];
         job = int(meta & 0xffu);
-        n_coh = int((meta >> 16) & 0x7fu);
+        n_coh = int((meta >> 16) & 0x3fu);
+        spar = (meta >> 22) & 1u;
         n_incoh = int((meta >> 23) & 0x7fu);
         kind = meta >> 30;
         const uint64_t seed = J.seed;
@@ -266,8 +271,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
         rng.h0 = S.h0[sl];
         rng.h1 = S.h1[sl];
         rng.n = S.rn[sl];
-        // the unused half of a Philox block is never drawn after an event: the next step
-        // starts a new block (HistoryRng::next_pair64)
+        // the unused half of an event block is never drawn after the event: the next
+        // interaction starts a new block (HistoryRng::align_event)
         rng.b0 = rng.b1 = 0u;
         steps = S.steps[sl];
         fetches = S.fetches[sl];
@@ -300,7 +305,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
         S.qz[sl] = p0.z;
         S.s[sl] = s;
         S.vox[sl] = uint32_t(vox);
-        S.meta[sl] = pack_meta(job, mat, n_coh, n_incoh, kKindCollide);
+        S.meta[sl] = pack_meta(job, mat, n_coh, n_incoh, kKindCollide, spar);
     };
     auto save_after_event = [&](int sl) {  // a photon leaving an event (or a new history)
         save_flight(sl);
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
         S.mumax[sl] = mu_max;
         S.h0[sl] = rng.h0;
         S.h1[sl] = rng.h1;
-        S.meta[sl] = pack_meta(job, mat, n_coh, n_incoh, kKindFlight);
+        S.meta[sl] = pack_meta(job, mat, n_coh, n_incoh, kKindFlight, spar);
     };
     // Compton trials go to the statistics at the event itself (sample_compton counts them)
     auto end_history = [&]() {
@@ -383,12 +388,29 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
                     stat_add(st, kStStepCap, 1);
                     park = kKindStart;
                 } else {
+                    // the step's uniforms: the word pair (0, 1) of its block for an even step
+                    // index, (2, 3) for an odd one.  A flight segment starts even and passes
+                    // run two steps, so a pass computes one block and its second step takes
+                    // the pair kept from the first; a step of odd index in a pass's first
+                    // step (one step per pass, or a segment start in mid-pass) recomputes.
+                    const uint32_t si = steps + spar;
                     ++steps;
-                    uint64_t w1, w2;
-                    if constexpr (MULTI)
-                        rng.next_pair64_rk(w1, w2, s_rk);
-                    else
-                        rng.next_pair64_rk(w1, w2, P.round_keys);
+                    uint32_t wa, wb;
+                    if (pass == 0 || !(si & 1u)) {
+                        Philox4 q;
+                        if constexpr (MULTI)
+                            q = rng.step_block_rk(si, s_rk);
+                        else
+                            q = rng.step_block_rk(si, P.round_keys);
+                        wa = (si & 1u) ? q.v[2] : q.v[0];
+                        wb = (si & 1u) ? q.v[3] : q.v[1];
+                        sw2 = q.v[2];
+                        sw3 = q.v[3];
+                    } else {
+                        wa = sw2;
+                        wb = sw3;
+                    }
+                    const uint64_t w1 = uint64_t(wa) << 32, w2 = uint64_t(wb) << 32;
                     // MIDSX_TRACK_BACKGROUND_FAST: a photon known to be in the background (vox == -1
                     // after its last voxel lookup) flies against the background's own attenuation,
                     // exact there, up to the first grid it would enter
@@ -524,6 +546,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
                 const R mu_tot = S.mu[mat * ns + sl];
                 R p_coh, p_incoh;
                 interaction_probs<R>(P.T, Mt, E, mu_tot, p_coh, p_incoh);
+                rng.align_event();
                 const R u3 = uniform<R>(rng);
                 cls0 = scatter_class(n_coh, n_incoh);
                 E0 = E;
@@ -587,6 +610,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
                         }
                     }
                 }
+                spar = steps & 1u;  // a new flight segment (HistoryRng)
                 ended = finish;
             }
         }
@@ -632,6 +656,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
                     stat_add(sj, kStSourceE, fx_stat(E));
                     n_coh = n_incoh = 0;
                     steps = fetches = trials = words = 0;
+                    spar = 0u;
                     mat = 0;
                     vox = -2;  // region of the source point not looked up yet
                     s = R(0);

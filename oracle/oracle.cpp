@@ -90,22 +90,57 @@ static inline void philox10(uint32_t* c, uint32_t k0, uint32_t k1) {
     }
 }
 
+// The device's stream definition (Philox mode), restated: a history id h and the run's seed
+// (the key) give two kinds of draws.
+//   * Event draws (source, interaction type, samplers, azimuths): 64-bit values, draw n being
+//     the half (n & 1) of block (n >> 1, h_lo, h_hi, 0).  Each interaction starts a new
+//     block (n rounded up to even).
+//   * Woodcock-step draws: the step's two uniforms (free path, delta test) are the 32-bit
+//     word pair (2 (i & 1), 2 (i & 1) + 1) of block (i >> 1, h_lo, h_hi, 1 + n), n the event
+//     draws made so far - constant along a flight segment (the steps between two
+//     interactions), different for every segment - and i = (Woodcock steps of the history
+//     so far) + p, p the parity of that count at the segment's start, so that every segment
+//     starts on a block boundary.  Two steps thus share one block.
 struct Generator {
     int mode = RNG_PHILOX;
     // Philox history stream
     uint64_t seed = 0, history = 0;
     uint64_t draws = 0;
+    uint64_t steps = 0;    // Woodcock steps of the history so far
+    uint64_t parity = 0;   // of `steps` at the start of the current flight segment
+    double step_u[2] = {0, 0};
+    int step_left = 0;     // step uniforms not yet handed out by next()
     // mt19937 thread stream
     std::mt19937 mt;
     std::uniform_real_distribution<double> unit{0.0, 1.0};
 
-    // The free-path draw of each Woodcock step starts a new Philox block (even draw index),
-    // so that a step's two draws share one block (the device's stream definition).
-    void alignStep() {
+    void startHistory(uint64_t h) {
+        history = h;
+        draws = 0;
+        steps = 0;
+        parity = 0;
+        step_left = 0;
+    }
+    // A Woodcock step: its free-path and delta-test uniforms become the next two next() values.
+    void beginStep() {
+        if (mode != RNG_PHILOX) return;
+        const uint64_t i = steps + parity;
+        uint32_t c[4] = {uint32_t(i >> 1), uint32_t(history), uint32_t(history >> 32), uint32_t(1u + draws)};
+        philox10(c, uint32_t(seed), uint32_t(seed >> 32));
+        const int w = (i & 1) ? 2 : 0;
+        for (int k = 0; k < 2; ++k) step_u[k] = double(((uint64_t(c[w + k]) << 32) >> 11) + 1) * (1.0 / 9007199254740992.0);
+        step_left = 2;
+        ++steps;
+    }
+    // An interaction: its draws start on a block boundary.
+    void beginEvent() {
         if (mode == RNG_PHILOX && (draws & 1)) ++draws;
     }
+    // A photon that leaves an interaction starts a new flight segment.
+    void beginSegment() { parity = steps & 1; }
     double next() {
         if (mode == RNG_MT19937) return unit(mt);
+        if (step_left) return step_u[2 - step_left--];
         uint32_t c[4] = {uint32_t(draws >> 1), uint32_t(history), uint32_t(history >> 32), 0u};
         philox10(c, uint32_t(seed), uint32_t(seed >> 32));
         uint64_t r = (draws & 1) ? ((uint64_t(c[2]) << 32) | c[3]) : ((uint64_t(c[0]) << 32) | c[1]);
@@ -633,7 +668,7 @@ struct PhysicsEngine {
     PhysicsEngine(const ComputationalDomain& d, const InteractionData& i) : dom(d), data(i) {}
 
     double getFreePath(double mu_max) {
-        tl_gen->alignStep();
+        tl_gen->beginStep();
         return -std::log(uniform_dist_.sample()) / mu_max;
     }
     bool isDeltaScatter(double mu, double mu_max) {
@@ -683,6 +718,7 @@ struct PhysicsEngine {
         double mu = m.total(E);
         if (!isDeltaScatter(mu, mu_max)) {
             sd.isInteract = vd.isInteract = true;
+            tl_gen->beginEvent();
             setInteractionType(photon, m, mu);
             photon.isPrimary = false;
             auto* beh = photon.behavior.get();
@@ -691,6 +727,7 @@ struct PhysicsEngine {
             else tl_cnt->incoh++;
             double dep = photon.interact(m);
             if (photon.failed) return;  // table range or trial cap: drop the history's step
+            if (!photon.terminated) tl_gen->beginSegment();
             vd.energy_deposited = dep;
             vd.final_photon = photon;
             tx.push_back({voxel, dep});
@@ -929,8 +966,7 @@ int run_domain(const midsx_table_blob* blob, ref::ComputationalDomain& dom, size
         engine.max_steps = steps_cap;
 #pragma omp for schedule(static)
         for (int64_t i = 0; i < int64_t(n); ++i) {
-            st.gen.history = first + uint64_t(i);
-            st.gen.draws = 0;
+            st.gen.startHistory(first + uint64_t(i));
             Photon photon = source.generatePhoton();
             st.cnt.histories++;
             st.cnt.source_e += photon.energy;
@@ -1126,8 +1162,7 @@ int oracle_sample(const midsx_table_blob* blob, int kind, int material, double e
         IncoherentScattering inc;
 #pragma omp for schedule(static)
         for (int64_t i = 0; i < n; ++i) {
-            gen.history = first + uint64_t(i);
-            gen.draws = 0;
+            gen.startHistory(first + uint64_t(i));
             if (kind == 0) {
                 double mu;
                 out0[i] = m.rayleigh.sample(energy, mu) ? mu : NAN;

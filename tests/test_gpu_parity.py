@@ -176,7 +176,13 @@ def test_water_cube_against_independent_oracle(cube, precision):
     assert abs(st["deposited_grid"] - so["deposited_grid"]) / so["deposited_grid"] < 0.005
     assert abs(st["escaped_energy"] - so["escaped_energy"]) / so["escaped_energy"] < 0.005
     oe, oc = o["binned"][0]
-    assert abs(be.sum() - oe.sum()) / oe.sum() < 0.005
+    # exit-plane total: within 0.5 %, or within 4 sigma where the sample cannot resolve 0.5 %
+    # (at 4e5 histories the two runs' totals differ by ~0.45 % at one sigma); sigma from the
+    # bins' Poisson-compound variances, tot^2 / count per bin
+    cg, co = bc.sum(axis=2).ravel(), oc.sum(axis=2).ravel()
+    tg, to = be.sum(axis=2).ravel(), oe.sum(axis=2).ravel()
+    var = (tg[cg > 0] ** 2 / cg[cg > 0]).sum() + (to[co > 0] ** 2 / co[co > 0]).sum()
+    assert abs(be.sum() - oe.sum()) < max(0.005 * oe.sum(), 4 * np.sqrt(var)), (be.sum(), oe.sum(), np.sqrt(var))
     z = chi_voxels(d["sum"].ravel(), d["sumsq"].ravel(), o["dose"]["sum"].ravel(), o["dose"]["sumsq"].ravel())
     assert z.size > 50
     assert np.mean(np.abs(z) > 3) < 0.01, np.mean(np.abs(z) > 3)
