@@ -356,9 +356,9 @@ typedef struct midsx_run_config {
     int32_t tracking;            /* midsx_tracking */
     int32_t steps_per_pass;      /* batched photon-pool launches: Woodcock steps a lane takes
                                     between the warp's list bookkeeping, 1..4 (0 = tuned
-                                    default: 2 for the FP32 form with reference tracking, else
-                                    1; the request server's default is 1).  Single runs use
-                                    the default, fixed at compile time. */
+                                    default: 2 for the FP32 form with reference tracking, the
+                                    request server's launches included, else 1).  Single runs
+                                    use the default, fixed at compile time. */
     int32_t variance_batches;    /* MIDSX_DOSE_BATCHES tallies: batches this run is split into
                                     (0 or 1: the run is one batch); at most 1024 */
     int32_t pass_repeats;        /* batched photon-pool launches: passes repeated without the

@@ -23,8 +23,9 @@ constexpr int kPoolSlots = 64;        // photon slots per warp
 // (ready and event lists, ballots) runs.  Single-job kernels fix it at compile time (a
 // run-time bound cost the cone-beam dose workload 1 %): 2 for the FP32 form with reference
 // tracking, else 1 (default_steps_per_pass in transport.cu gives the measurements); batched
-// kernels take RunParams::steps_per_pass (the request server's mixed launches want 1, the
-// 64-job batch 2, the autotuner tries both).  A photon that parks ends its pass early.
+// kernels take RunParams::steps_per_pass (2 by default for the mixed form with reference
+// tracking, the request server's launches included; the autotuner tries 1 and 2).  A photon
+// that parks ends its pass early.
 template <typename R, int TRACK>
 __host__ __device__ constexpr int single_job_steps_per_pass() {
     return TRACK == MIDSX_TRACK_REFERENCE && sizeof(R) == 4 ? 2 : 1;

@@ -166,16 +166,20 @@ __device__ __forceinline__ const Geo<double>& job0_geo(const RunParams& P, doubl
 
 // Default Woodcock steps per pass of the photon-pool loop.  FP32 reference tracking: 2
 // against 1 measured +5.5 to +10 % on the cone-beam dose workload and +6 % on the 64-job
-// batch (3, 4 and 6 were slower than 1).  The FP64 form (-2.3 % with 2), the opt-in modes
-// whose steps are long (a background flight, a cell walk; -8 to -9 % with 2) and the request
-// server's short mixed launches (-10 % histories/s, +12 % p99 latency with 2) keep one.
-// Batched launches: passes repeated between the pool's list bookkeeping (pass_repeats in
-// kernel_pool.cuh); single-job launches fix it at compile time.
+// batch (3, 4 and 6 were slower than 1); a pass of two steps also computes one Philox block
+// for both (HistoryRng's step stream), which made two steps pay for the request server's
+// short mixed launches too (+11 % histories/s at 200 requests/s, lower p50 and p99 for every
+// class; with one step per pass and one block per step they had measured -10 %).  The FP64
+// form (-2.3 % with 2) and the opt-in modes whose steps are long (a background flight, a
+// cell walk; -8 to -9 % with 2) keep one.  Batched launches: passes repeated between the
+// pool's list bookkeeping (pass_repeats in kernel_pool.cuh; the server's launches take one
+// repeat); single-job launches fix both at compile time.
 inline int default_pass_repeats(int precision, int tracking, bool server) {
     return precision == MIDSX_PREC_MIXED && tracking == MIDSX_TRACK_REFERENCE && !server ? 8 : 1;
 }
 inline int default_steps_per_pass(int precision, int tracking, bool server) {
-    return precision == MIDSX_PREC_MIXED && tracking == MIDSX_TRACK_REFERENCE && !server ? 2 : 1;
+    (void)server;
+    return precision == MIDSX_PREC_MIXED && tracking == MIDSX_TRACK_REFERENCE ? 2 : 1;
 }
 
 // -------------------------------------------------------------------- atomics ---
