@@ -272,9 +272,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
         rng.h0 = S.h0[sl];
         rng.h1 = S.h1[sl];
         rng.n = S.rn[sl];
-        // the unused half of an event block is never drawn after the event: the next
+        // the unused words of an event block are never drawn after the event: the next
         // interaction starts a new block (HistoryRng::align_event)
-        rng.b0 = rng.b1 = 0u;
+        rng.b1 = rng.b2 = rng.b3 = 0u;
         steps = S.steps[sl];
         fetches = S.fetches[sl];
         words = S.words[sl];

@@ -92,9 +92,9 @@ static inline void philox10(uint32_t* c, uint32_t k0, uint32_t k1) {
 
 // The device's stream definition (Philox mode), restated: a history id h and the run's seed
 // (the key) give two kinds of draws.
-//   * Event draws (source, interaction type, samplers, azimuths): 64-bit values, draw n being
-//     the half (n & 1) of block (n >> 1, h_lo, h_hi, 0).  Each interaction starts a new
-//     block (n rounded up to even).
+//   * Event draws (source, interaction type, samplers, azimuths): draw n is the 32-bit word
+//     (n & 3) of block (n >> 2, h_lo, h_hi, 0).  Each interaction starts a new block (n
+//     rounded up to a multiple of 4).
 //   * Woodcock-step draws: the step's two uniforms (free path, delta test) are the 32-bit
 //     word pair (2 (i & 1), 2 (i & 1) + 1) of block (i >> 1, h_lo, h_hi, 1 + n), n the event
 //     draws made so far - constant along a flight segment (the steps between two
@@ -134,16 +134,16 @@ struct Generator {
     }
     // An interaction: its draws start on a block boundary.
     void beginEvent() {
-        if (mode == RNG_PHILOX && (draws & 1)) ++draws;
+        if (mode == RNG_PHILOX) draws = (draws + 3) & ~uint64_t(3);
     }
     // A photon that leaves an interaction starts a new flight segment.
     void beginSegment() { parity = steps & 1; }
     double next() {
         if (mode == RNG_MT19937) return unit(mt);
         if (step_left) return step_u[2 - step_left--];
-        uint32_t c[4] = {uint32_t(draws >> 1), uint32_t(history), uint32_t(history >> 32), 0u};
+        uint32_t c[4] = {uint32_t(draws >> 2), uint32_t(history), uint32_t(history >> 32), 0u};
         philox10(c, uint32_t(seed), uint32_t(seed >> 32));
-        uint64_t r = (draws & 1) ? ((uint64_t(c[2]) << 32) | c[3]) : ((uint64_t(c[0]) << 32) | c[1]);
+        const uint64_t r = uint64_t(c[draws & 3]) << 32;
         ++draws;
         return double((r >> 11) + 1) * (1.0 / 9007199254740992.0);
     }

@@ -131,7 +131,9 @@ def test_macro_cells_radiography_with_lead(precision):
     ka, kb = ca.sum(axis=2).ravel(), cb.sum(axis=2).ravel()
     sel = (ka + kb) > 200
     zb = (ta[sel] - tb[sel]) / np.sqrt(ta[sel] ** 2 / ka[sel] + tb[sel] ** 2 / kb[sel])
-    assert np.mean(np.abs(zb) > 4) < 0.01
+    # tot^2 / count understates a bin's variance when its energies spread (scatter), so a
+    # 4-sigma bin is not rare enough to forbid among a few dozen: one is allowed, or 1 %
+    assert np.sum(np.abs(zb) > 4) <= max(1, int(0.01 * zb.size)), (zb.size, np.sort(np.abs(zb))[-3:])
 
 
 def test_macro_cells_overlapping_grids():
