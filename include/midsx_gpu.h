@@ -374,7 +374,10 @@ typedef struct midsx_run_config {
 /* Transports n_histories photons and accumulates into `tallies` (asynchronous on stream).
  * Replaces runSimulation's history loop (src/MIDSX/Core/run_simulation.cpp:13-35).
  * Random numbers: Philox4x32-10 keyed by seed, one counter stream per history id, so a
- * run split into several calls over disjoint history ranges equals one call. */
+ * run split into several calls over disjoint history ranges equals one call.  Every draw is
+ * a 32-bit word: an interaction's draws (interaction type, samplers, azimuth) come four to a
+ * block, starting a new block; a flight segment's Woodcock steps (free path, delta test) two
+ * to a block of a counter range of their own.  Both precisions draw the same words. */
 midsx_status midsx_gpu_run(midsx_tables_h tables, midsx_phantom_h phantom, midsx_source_h source,
                            midsx_tallies_h tallies, const midsx_run_config* cfg, void* stream);
 
