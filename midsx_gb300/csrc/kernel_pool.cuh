@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) transport_pool_ke
                     } else if constexpr (MX) {
                         s = fmaxf(-__logf(to_uniform(w1, R(0))), 0.0f) * inv_mu_max;
                     } else {
-                        s = -log_(to_uniform(w1, R(0))) / mu_max;
+                        s = -log_(to_uniform(w1, R(0))) * inv_mu_max;
                     }
                     p0 = pos;
                     pos = {pos.x + s * dir.x, pos.y + s * dir.y, pos.z + s * dir.z};
