@@ -258,17 +258,11 @@ MIDSX_HD V3<R> rotate_half(const V3<R>& v, R st, R ct, R sp, R cp) {
         p = {-v.y, v.x, R(0)};
     }
     R pn = sqrt_(dot(p, p));
-    if (pn > R(0)) {
-        if constexpr (sizeof(R) == 4) {  // FP32: one division
-            const R ipn = R(1) / pn;
-            p.x *= ipn;
-            p.y *= ipn;
-            p.z *= ipn;
-        } else {
-            p.x /= pn;
-            p.y /= pn;
-            p.z /= pn;
-        }
+    if (pn > R(0)) {  // one division
+        const R ipn = R(1) / pn;
+        p.x *= ipn;
+        p.y *= ipn;
+        p.z *= ipn;
     }
     // q_theta = (ct, p st), q_phi = (cp, v sp)
     R tw = ct, tx = p.x * st, ty = p.y * st, tz = p.z * st;
@@ -285,13 +279,8 @@ MIDSX_HD V3<R> rotate_half(const V3<R>& v, R st, R ct, R sp, R cp) {
     R rz = qw * v.z + qx * v.y - qy * v.x;
     // q^-1 = conj(q) / |q|^2
     R n2 = qw * qw + qx * qx + qy * qy + qz * qz;
-    R iw, ix, iy, iz;
-    if constexpr (sizeof(R) == 4) {  // FP32: one division
-        const R in2 = R(1) / n2;
-        iw = qw * in2, ix = -qx * in2, iy = -qy * in2, iz = -qz * in2;
-    } else {
-        iw = qw / n2, ix = -qx / n2, iy = -qy / n2, iz = -qz / n2;
-    }
+    const R in2 = R(1) / n2;  // one division
+    const R iw = qw * in2, ix = -qx * in2, iy = -qy * in2, iz = -qz * in2;
     // out = r * q^-1 (vector part)
     V3<R> o;
     o.x = rw * ix + rx * iw + ry * iz - rz * iy;

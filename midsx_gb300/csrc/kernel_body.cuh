@@ -20,9 +20,10 @@
 
 // per-energy cache: majorant and every material's total cross section and delta-scatter
 // threshold (isDeltaScatter: p_delta = 1 - mu / mu_max), kept per thread in shared memory.
-// The FP32 form multiplies by one reciprocal of the majorant instead of dividing per material
-// (with the same change in interaction_probs and rotate_half: +9.3 % on the cone-beam dose
-// workload; the thresholds move by an ulp, the Woodcock steps per history by 3e-9).
+// Both forms multiply by one reciprocal of the majorant instead of dividing per material
+// (with the same change in interaction_probs, rotate_half and the source direction: FP32
+// +9.3 %, FP64 +4.6 % with the Compton trial below, on the cone-beam dose workload; the
+// thresholds move by an ulp, the Woodcock steps per history by 3e-9).
 template <typename R>
 __device__ __forceinline__ R refresh_energy(const RunParams& P, R E, R* thr, R* mu, int stride) {
     const EnergyKey<R> key = energy_key<R>(P.T, E);  // one log10 and bucket for every table
@@ -31,10 +32,7 @@ __device__ __forceinline__ R refresh_energy(const RunParams& P, R E, R* thr, R* 
     for (int m = 0; m < P.T.n_materials; ++m) {
         R mm = lin_lookup_key<R>(P.T, P.T.mat[m].total, key);
         mu[m * stride] = mm;
-        if constexpr (sizeof(R) == 4)
-            thr[m * stride] = R(1) - mm * imax;
-        else
-            thr[m * stride] = R(1) - mm / mu_max;
+        thr[m * stride] = R(1) - mm * imax;
     }
     return mu_max;
 }
@@ -62,14 +60,9 @@ __device__ __forceinline__ void interaction_probs(const DevTables& T, const DevM
         if (w) incoh = v;
         else coh = v;
     }
-    if constexpr (sizeof(R) == 4) {
-        const R im = R(1) / mu_tot;  // FP32: one division (the FP64 form divides as the reference)
-        p_coh = coh * im;
-        p_incoh = incoh * im;
-    } else {
-        p_coh = coh / mu_tot;
-        p_incoh = incoh / mu_tot;
-    }
+    const R im = R(1) / mu_tot;  // one division for both probabilities
+    p_coh = coh * im;
+    p_incoh = incoh * im;
 }
 
 // scatter_direction for the coherent and incoherent branches.
@@ -91,52 +84,31 @@ __device__ __forceinline__ bool sample_compton(const RunParams& P, const DevMate
     const R k = E / R(kMec2);
     const R r1p = (R(1) + R(2) * k) / (R(9) + R(2) * k);
     const R s_max = lin_lookup<R>(P.T, Mt.sfunc, alpha * k * sqrt_(R(2)));
-    if constexpr (sizeof(R) == 4) {
-        // The same trial with one division instead of six to eight: with b = 1 + 2k r2 and
-        // a = 1 + 2k, chi = b (first branch) or a / b (second), 1/chi = b / a there, and
-        // 1/k - 1/kp = (1 - chi)/k; 1/k, 1/a and 1/s_max are taken once per event.  Equal to
-        // the form below up to rounding (+2.5 % on the cone-beam dose workload); the FP64
-        // form keeps the reference's expressions, operation for operation.
-        const R ik = R(1) / k, k2 = R(2) * k, a = R(1) + k2, ia = R(1) / a, is_max = R(1) / s_max;
-        for (int trial = 0; trial < P.max_trials; ++trial) {
-            ++trials;
-            R r1 = uniform<R>(rng), r2 = uniform<R>(rng), r3 = uniform<R>(rng);
-            R chi, ichi;
-            const R b = R(1) + k2 * r2;
-            if (r1 <= r1p) {
-                chi = b;
-                ichi = R(1) / chi;
-                if (!(r3 <= R(4) * ichi * (R(1) - ichi))) continue;
-            } else {
-                ichi = b * ia;
-                chi = a / b;
-                R tt = (R(1) - chi) * ik + R(1);
-                if (!(R(2) * r3 <= tt * tt + ichi)) continue;
-            }
-            kp = k * ichi;
-            mu = R(1) + (R(1) - chi) * ik;
-            R x = alpha * k * sqrt_(R(1) - mu);
-            R accept = lin_lookup<R>(P.T, Mt.sfunc, x) * is_max;
-            if (uniform<R>(rng) <= accept) return true;
-        }
-        return false;
-    }
+    // Kahn's trial (photon_interactions.cpp:62-141) with one division instead of six to eight:
+    // with b = 1 + 2k r2 and a = 1 + 2k, chi = b (first branch) or a / b (second), 1/chi = b / a
+    // there, and 1/k - 1/kp = (1 - chi)/k; 1/k, 1/a and 1/s_max are taken once per event.
+    // Equal to the reference's expressions up to rounding (FP32 +2.5 % on the cone-beam dose
+    // workload; FP64 histories still equal the oracle's, which keeps them, to 1e-9).
+    const R ik = R(1) / k, k2 = R(2) * k, a = R(1) + k2, ia = R(1) / a, is_max = R(1) / s_max;
     for (int trial = 0; trial < P.max_trials; ++trial) {
         ++trials;
         R r1 = uniform<R>(rng), r2 = uniform<R>(rng), r3 = uniform<R>(rng);
-        R chi;
+        R chi, ichi;
+        const R b = R(1) + k2 * r2;
         if (r1 <= r1p) {
-            chi = R(1) + R(2) * k * r2;
-            if (!(r3 <= R(4) * (R(1) / chi - R(1) / (chi * chi)))) continue;
+            chi = b;
+            ichi = R(1) / chi;
+            if (!(r3 <= R(4) * ichi * (R(1) - ichi))) continue;
         } else {
-            chi = (R(1) + R(2) * k) / (R(1) + R(2) * k * r2);
-            R tt = R(1) / k - chi / k + R(1);
-            if (!(R(2) * r3 <= tt * tt + R(1) / chi)) continue;
+            ichi = b * ia;
+            chi = a / b;
+            R tt = (R(1) - chi) * ik + R(1);
+            if (!(R(2) * r3 <= tt * tt + ichi)) continue;
         }
-        kp = k / chi;
-        mu = R(1) + R(1) / k - R(1) / kp;
+        kp = k * ichi;
+        mu = R(1) + (R(1) - chi) * ik;
         R x = alpha * k * sqrt_(R(1) - mu);
-        R accept = lin_lookup<R>(P.T, Mt.sfunc, x) / s_max;
+        R accept = lin_lookup<R>(P.T, Mt.sfunc, x) * is_max;
         if (uniform<R>(rng) <= accept) return true;
     }
     return false;

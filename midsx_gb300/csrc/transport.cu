@@ -404,12 +404,8 @@ __device__ __forceinline__ void sample_source(const DevSource& S, HistoryRng& rn
         }
     }
     R nd = sqrt_(dot(d, d));
-    if constexpr (sizeof(R) == 4) {  // FP32: one division
-        const R ind = R(1) / nd;
-        dir = {d.x * ind, d.y * ind, d.z * ind};
-    } else {
-        dir = {d.x / nd, d.y / nd, d.z / nd};
-    }
+    const R ind = R(1) / nd;  // one division
+    dir = {d.x * ind, d.y * ind, d.z * ind};
     if (S.spec_kind == MIDSX_SPEC_MONO) {
         if constexpr (sizeof(R) == 8)
             E = S.mono;
