@@ -680,7 +680,7 @@ def batched_leg(args, torch):
     stream.synchronize()
     persistent_s = ev[0].elapsed_time(ev[1]) / 1e3 / reps
     batch.set_own_launch(0)
-    own_min = 57344 * torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    own_min = 28672 * torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     # the same jobs as separate single-simulation launches
     ev2 = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     ev2[0].record(ts)

@@ -458,8 +458,8 @@ midsx_status midsx_gpu_batch_destroy(midsx_batch_h b);
  * captured graph); results are unchanged (same history ids and streams).  A long job gains
  * nothing from sharing a launch - its own launch's tail is a small share of its time - and
  * runs faster in the single-job kernel, whose job lives in the constant bank instead of
- * shared memory.  0 restores the default, 32 loads of the GPU's resident photon slots
- * (57,344 histories per SM: 8.7e6 on 152 SMs); UINT64_MAX keeps every job in the persistent
+ * shared memory.  0 restores the default, 16 loads of the GPU's resident photon slots
+ * (28,672 histories per SM: 4.4e6 on 152 SMs); UINT64_MAX keeps every job in the persistent
  * launch.  Synchronous; call it outside a stream capture. */
 midsx_status midsx_gpu_batch_set_own_launch(midsx_batch_h b, uint64_t min_histories);
 /* One persistent launch over every job (cfg: precision and launch shape; its seed/first/n are
