@@ -66,6 +66,8 @@ def load():
                                            C.POINTER(C.c_int64)]
         lib.oracle_philox.restype = None
         lib.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        lib.oracle_generator_script.restype = C.c_int
+        lib.oracle_generator_script.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_int32), C.c_int64, PD]
         _lib = lib
     return _lib
 
@@ -212,6 +214,21 @@ def philox(ctr, key):
     o = (C.c_uint32 * 4)()
     lib.oracle_philox(c, k, o)
     return list(o)
+
+
+GEN_DRAW, GEN_EVENT, GEN_STEP, GEN_SEGMENT = 0, 1, 2, 3
+
+
+def generator_script(seed, history, ops):
+    """The oracle's Philox-mode generator of one history driven by `ops` (GEN_*): the values
+    of its draws, in order."""
+    lib = load()
+    ops = np.ascontiguousarray(ops, dtype=np.int32)
+    out = np.empty(int(np.sum(ops == GEN_DRAW)))
+    if lib.oracle_generator_script(int(seed), int(history), ops.ctypes.data_as(C.POINTER(C.c_int32)), ops.size,
+                                   N.dptr(out)) != 0:
+        raise RuntimeError("oracle_generator_script: unknown op")
+    return out
 
 
 def tables_for(scene):

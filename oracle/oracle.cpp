@@ -1220,4 +1220,25 @@ void oracle_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
     for (int i = 0; i < 4; ++i) out[i] = c[i];
 }
 
+/* The Philox-mode generator of one history driven by a script, for tests of its draw
+ * layout: op 0 = one draw (event draw, or the next step uniform after op 2), 1 =
+ * beginEvent, 2 = beginStep, 3 = beginSegment.  out receives every draw's value. */
+int oracle_generator_script(uint64_t seed, uint64_t history, const int32_t* ops, int64_t n_ops, double* out) {
+    ref::Generator g;
+    g.mode = ref::RNG_PHILOX;
+    g.seed = seed;
+    g.startHistory(history);
+    int64_t k = 0;
+    for (int64_t i = 0; i < n_ops; ++i) {
+        switch (ops[i]) {
+            case 0: out[k++] = g.next(); break;
+            case 1: g.beginEvent(); break;
+            case 2: g.beginStep(); break;
+            case 3: g.beginSegment(); break;
+            default: return 1;
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"

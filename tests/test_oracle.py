@@ -37,6 +37,69 @@ def test_philox_known_answers(ctr, key, expect):
     assert oracle.philox(ctr, key) == expect
 
 
+# ------------------------------------------------------------ stream layout ---
+def _philox_py(ctr, key):
+    """Philox4x32-10 (Salmon et al., SC'11) in plain Python, independent of the oracle."""
+    x = list(ctr)
+    k0, k1 = key
+    M = 0xFFFFFFFF
+    for r in range(10):
+        if r:
+            k0, k1 = (k0 + 0x9E3779B9) & M, (k1 + 0xBB67AE85) & M
+        p0, p1 = 0xD2511F53 * x[0], 0xCD9E8D57 * x[2]
+        x = [(p1 >> 32) ^ x[1] ^ k0, p1 & M, (p0 >> 32) ^ x[3] ^ k1, p0 & M]
+    return x
+
+
+def _u(word):
+    return (((word << 32) >> 11) + 1) * 2.0 ** -53
+
+
+def test_generator_follows_the_documented_draw_layout():
+    """The history stream the device and the oracle share: event draw n is word (n & 3) of
+    block (n >> 2, h_lo, h_hi, 0), each interaction starting a new block; the Woodcock-step
+    pair of step index i is words (2 (i & 1), 2 (i & 1) + 1) of block (i >> 1, h_lo, h_hi,
+    1 + n), i = steps so far + the parity they had at the flight segment's start."""
+    seed, h = 0x0123456789ABCDEF, 0x0000000A00000007
+    key = (seed & 0xFFFFFFFF, seed >> 32)
+    hl, hh = h & 0xFFFFFFFF, h >> 32
+    D, E, S, G = oracle.GEN_DRAW, oracle.GEN_EVENT, oracle.GEN_STEP, oracle.GEN_SEGMENT
+    # a history: 3 source draws, 3 steps, an interaction (5 draws), a segment, 2 steps,
+    # an interaction (2 draws), a segment, 1 step
+    ops = [D, D, D] + [S, D, D] * 3 + [E] + [D] * 5 + [G] + [S, D, D] * 2 + [E, D, D, G] + [S, D, D]
+    got = oracle.generator_script(seed, h, ops)
+    want, n, steps, par = [], 0, 0, 0
+
+    def event():
+        nonlocal n
+        w = _philox_py([n >> 2, hl, hh, 0], key)[n & 3]
+        n += 1
+        return _u(w)
+
+    def step():
+        nonlocal steps
+        i = steps + par
+        b = _philox_py([i >> 1, hl, hh, 1 + n], key)
+        steps += 1
+        o = 2 * (i & 1)
+        return [_u(b[o]), _u(b[o + 1])]
+
+    want += [event() for _ in range(3)]
+    for _ in range(3):
+        want += step()
+    n = (n + 3) & ~3
+    want += [event() for _ in range(5)]
+    par = steps & 1
+    for _ in range(2):
+        want += step()
+    n = (n + 3) & ~3
+    want += [event() for _ in range(2)]
+    par = steps & 1
+    want += step()
+    assert len(got) == len(want)
+    np.testing.assert_array_equal(got, np.array(want))
+
+
 # ----------------------------------------------------------- HVL golden results ---
 def hvl_primary(blob, golden, case, kind, n, seed, rng=oracle.RNG_PHILOX):
     sc = golden["scene"]
