@@ -316,6 +316,7 @@ struct DevTables {
     const double* d;     // FP64 data (blob layout)
     const float* f;      // FP32 copy, same offsets
     const float* fs;     // FP32 LogLogLinear slopes at the ly offsets (lin_eval_slope_at_log)
+    const double* ds;    // the same slopes in FP64: the quotient the FP64 lookup would compute
     const int* rows;     // RITA row starts
     const int* bk;       // bucket tables of every searched node array
     BucketSpec bs[2][2];  // [kind][0 = FP64 query, 1 = FP32 query]
@@ -336,6 +337,18 @@ MIDSX_HD const double* tab<double>(const DevTables& t) {
 template <>
 MIDSX_HD const float* tab<float>(const DevTables& t) {
     return t.f;
+}
+// LogLogLinear slopes of the working precision (tables_create: FP64 quotients, and their
+// FP32 roundings)
+template <typename R>
+MIDSX_HD const R* slopes(const DevTables& t);
+template <>
+MIDSX_HD const double* slopes<double>(const DevTables& t) {
+    return t.ds;
+}
+template <>
+MIDSX_HD const float* slopes<float>(const DevTables& t) {
+    return t.fs;
 }
 
 template <typename R>
@@ -362,12 +375,10 @@ template <typename R>
 MIDSX_HD R lin_lookup(const DevTables& t, const DevLin& L, R q) {
     const R* D = tab<R>(t);
     const int idx = lin_index_bk<R>(t, L, q);
-    if constexpr (sizeof(R) == 4) {
-        if (idx == 0 || idx >= L.n) return lin_eval_slope_at_log(D + L.lx, D + L.ly, t.fs + L.ly, L.n, idx, R(0));
-        return lin_eval_slope_at_log(D + L.lx, D + L.ly, t.fs + L.ly, L.n, idx, log10_(q));
-    } else {
-        return lin_eval_at(D + L.lx, D + L.ly, L.n, idx, q);
-    }
+    // slopes from the host: FP32 rounded once from FP64; FP64 the same quotient the device
+    // would divide out per lookup, bit for bit (one division less per FP64 lookup)
+    if (idx == 0 || idx >= L.n) return lin_eval_slope_at_log(D + L.lx, D + L.ly, slopes<R>(t) + L.ly, L.n, idx, R(0));
+    return lin_eval_slope_at_log(D + L.lx, D + L.ly, slopes<R>(t) + L.ly, L.n, idx, log10_(q));
 }
 
 // Knot span with the bucketed search (same result as spline_span).
@@ -422,10 +433,7 @@ MIDSX_HD R lin_lookup_key(const DevTables& t, const DevLin& L, const EnergyKey<R
         const int* st = buckets<R>(t, L.bk_d, L.bk_f);
         idx = upper_index(x, st[k.b], st[k.b + 1], k.q);
     }
-    if constexpr (sizeof(R) == 4)
-        return lin_eval_slope_at_log(D + L.lx, D + L.ly, t.fs + L.ly, L.n, idx, k.lq);
-    else
-        return lin_eval_at_log(D + L.lx, D + L.ly, L.n, idx, k.lq);
+    return lin_eval_slope_at_log(D + L.lx, D + L.ly, slopes<R>(t) + L.ly, L.n, idx, k.lq);
 }
 
 // spline_lookup with a precomputed key: same span, same value.

@@ -147,8 +147,9 @@ MIDSX_HD R lin_eval_at_log(const R* lx, const R* ly, int n, int idx, R lq) {
 }
 
 // LogLogLinear value on interval idx with the interval's slope given (sl[idx] for the interval
-// [idx - 1, idx]), for the FP32 tables: their slopes are computed in FP64 on the host and
-// rounded once.  Grid nodes closer than FP32 resolves in log10 (merged grids hold node pairs a
+// [idx - 1, idx]).  The slopes are computed in FP64 on the host: the FP64 lookups take them as
+// they are (the quotient lin_eval_at_log divides out, bit for bit), the FP32 lookups rounded
+// once.  Grid nodes closer than FP32 resolves in log10 (merged grids hold node pairs a
 // few meV apart) share one float log10 energy, a zero-width interval whose slope recomputed in
 // FP32 would be infinite; the stored slope stays finite, and no division is left on the device.
 template <typename R>

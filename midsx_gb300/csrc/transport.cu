@@ -558,6 +558,7 @@ struct midsx_gpu_tables {
     double* d = nullptr;
     float* f = nullptr;
     float* fs = nullptr;  // FP32 LogLogLinear slopes (computed in FP64), same offsets as d
+    double* ds = nullptr;  // the FP64 slopes themselves
     int* rows = nullptr;
     int* bk = nullptr;
     int32_t ids[MIDSX_MAX_MATERIALS];
@@ -823,10 +824,12 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
         d.rita.n_energy = s.rita.n_energy;
         h->ids[m] = s.id;
     }
-    // FP32 slopes of every LogLogLinear table: (ly[i] - ly[i-1]) / (lx[i] - lx[i-1]) in FP64,
-    // rounded once (0 where two nodes share a log10 energy even in FP64)
+    // Slopes of every LogLogLinear table: (ly[i] - ly[i-1]) / (lx[i] - lx[i-1]) in FP64 - the
+    // quotient an FP64 lookup computes, bit for bit (IEEE division) - and rounded once for the
+    // FP32 lookups (0 where two nodes share a log10 energy even in FP64)
     {
         std::vector<float> slopes(nd, 0.0f);
+        std::vector<double> dslopes(nd, 0.0);
         auto add = [&](const midsx_lin_table& L) {
             const double* lx = blob->data + L.lx;
             const double* ly = blob->data + L.ly;
@@ -834,6 +837,7 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
                 const double dx = lx[i] - lx[i - 1];
                 const double v = dx != 0.0 ? (ly[i] - ly[i - 1]) / dx : 0.0;
                 slopes[size_t(L.ly + i)] = std::isfinite(v) ? float(v) : 0.0f;
+                dslopes[size_t(L.ly + i)] = std::isfinite(v) ? v : 0.0;
             }
         };
         add(blob->majorant);
@@ -847,6 +851,9 @@ extern "C" midsx_status midsx_gpu_tables_create(const midsx_table_blob* blob, mi
         if (!cuda_ok(cudaMalloc(&h->fs, nd * sizeof(float)), "cudaMalloc")) return MIDSX_OOM;
         CUDA_TRY(cudaMemcpy(h->fs, slopes.data(), nd * sizeof(float), cudaMemcpyHostToDevice));
         T.fs = h->fs;
+        if (!cuda_ok(cudaMalloc(&h->ds, nd * sizeof(double)), "cudaMalloc")) return MIDSX_OOM;
+        CUDA_TRY(cudaMemcpy(h->ds, dslopes.data(), nd * sizeof(double), cudaMemcpyHostToDevice));
+        T.ds = h->ds;
     }
     // bucket tables for every searched node array, FP64 and FP32 queries
     BucketBuilder bb;
@@ -875,6 +882,7 @@ extern "C" midsx_status midsx_gpu_tables_destroy(midsx_tables_h t) {
     cudaFree(t->d);
     cudaFree(t->f);
     cudaFree(t->fs);
+    cudaFree(t->ds);
     cudaFree(t->rows);
     cudaFree(t->bk);
     delete t;
