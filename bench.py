@@ -680,6 +680,8 @@ def batched_leg(args, torch):
     stream.synchronize()
     persistent_s = ev[0].elapsed_time(ev[1]) / 1e3 / reps
     batch.set_own_launch(0)
+    # the library's default own-launch threshold (batch_split: 16 loads of the resident photon
+    # slots, 28,672 histories per SM), to report which jobs took launches of their own
     own_min = 28672 * torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     # the same jobs as separate single-simulation launches
     ev2 = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
